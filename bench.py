@@ -1,0 +1,363 @@
+#!/usr/bin/env python
+"""Throughput of the batched pairwise-alignment stage on GB300.
+
+Default workload (xdrop1m): seeded X-drop extension (x = 49, k = 6, up to two
+seeds) + global alignment with statistics + coverage/ANI filter over 1M
+synthetic candidate pairs from 200k proteins (lognormal lengths, median 250,
+clamp 30-1000; half homologs at 30-80 % identity), BLOSUM62 with PASTIS's gap
+parameters -11 / -2.  A step is one pass of the aligner over the whole batch.
+
+  value  GCUPS with inputs resident in HBM (device buffers, pg_align_device)
+  e2e    GCUPS through pg_align with pinned host buffers: pair upload and
+         result download inside the timed region
+
+--impl reference times the CPU restatement of the reference's SeqAn path
+(the oracle; SeqAn itself is absent from the reference checkout) on all host
+cores, on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GCUPS & alignments/s, batched SW/X-drop: GPU plain vs tuned+filtered vs CPU"
+DPX_OPS_PER_CELL = 4  # E, F, H add-max and the max with the third term, int32
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="xdrop1m", choices=["xdrop1m", "sw100k", "uneven10m"])
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="CPU work per baseline sample (seconds)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload_desc(name, n, scale):
+    base = {
+        "xdrop1m": "seeded X-drop (x=49, k=6, <=2 seeds) + global alignment + stats + "
+                   "coverage/ANI filter, %d candidate pairs over %d synthetic proteins "
+                   "(lognormal lengths median 250 clamp 30-1000, 50%% homologs at 30-80%% "
+                   "identity, 2%% indels)",
+        "sw100k": "affine Smith-Waterman + stats + coverage/ANI filter, %d pairs over %d "
+                  "synthetic proteins (lognormal lengths median 250 clamp 30-1000)",
+        "uneven10m": "seeded X-drop, %d pairs over %d proteins, lengths 80%% lognormal "
+                     "median 300 + 20%% uniform 1000-5000",
+    }[name]
+    from pastis_gb300 import synth
+    p = synth.PRESETS[name]
+    return base % (n, int(round(p["nseqs"] * scale)))
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_sample(w, mode, p, budget_s, threads):
+    """Oracle over a prefix of the pairs sized to about budget_s of CPU time."""
+    from oracle import oracle as O
+    codes = O.encode(bytes(w.ascii))
+    n = min(len(w.pairs), 500)
+    while True:
+        t = time.perf_counter()
+        out = O.batch(mode, codes, w.offs, codes, w.offs, w.pairs[:n], p, nthreads=threads)
+        dt = time.perf_counter() - t
+        if dt >= budget_s * 0.5 or n >= len(w.pairs):
+            cells = int(out["cells"].astype(np.uint64).sum())
+            return cells, n, dt
+        n = min(len(w.pairs), int(n * max(2.0, budget_s / max(dt, 1e-3) * 0.9)))
+
+
+def oracle_params(cfg):
+    from oracle import oracle as O
+    from pastis_gb300 import capi
+    first, ext, xg = capi.resolved_gaps(cfg)
+    return O.make_params(gap_first=first, gap_ext=ext, xdrop_gap=xg, xdrop=cfg.xdrop,
+                         seed_len=cfg.seed_len, seed_count=cfg.seed_count, tie=cfg.tie,
+                         flags=cfg.flags, cov_thr=cfg.cov_thr, ani_thr=cfg.ani_thr)
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, rank):
+    """CPU restatement of the reference path, all host cores, bounded sample per step."""
+    from oracle import oracle as O
+    from pastis_gb300 import capi, synth
+    if rank != 0:
+        return
+    O.build()
+    w = synth.generate(args.workload, seed=20260101, scale=args.scale)
+    mode = capi.MODE_SW if args.workload == "sw100k" else capi.MODE_XDROP
+    cfg = capi.config(mode)
+    p = oracle_params(cfg)
+    cores = host_cores()
+    # size one step to about 10 s of CPU time
+    cells, n, dt = cpu_sample(w, mode, p, 10.0, cores)
+    codes = O.encode(bytes(w.ascii))
+    sub = w.pairs[:n]
+    for _ in range(args.warmup):
+        O.batch(mode, codes, w.offs, codes, w.offs, sub[:max(1, n // 10)], p, nthreads=cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out = O.batch(mode, codes, w.offs, codes, w.offs, sub, p, nthreads=cores)
+    dt = time.perf_counter() - t0
+    cells = int(out["cells"].astype(np.uint64).sum())
+    gcups = cells * args.steps / dt / 1e9
+    sample = "first %d of %d pairs of the workload per step" % (n, len(w.pairs))
+    line = {
+        "metric": METRIC, "value": gcups, "unit": "GCUPS", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic",
+        "config": {"workload": args.workload + ": " + workload_desc(args.workload, len(w.pairs),
+                                                                    args.scale),
+                   "mode": "xdrop" if mode else "sw", "pairs_per_step": n},
+        "impl": "reference",
+        "alignments_per_s": n * args.steps / dt,
+        "cpu_baseline": {"value": gcups, "unit": "GCUPS", "cores": cores, "kind": "port",
+                         "sample": sample + "; the reference's SeqAn path cannot be built "
+                                            "(empty submodules), the oracle restates it"},
+        "e2e": {"value": gcups, "unit": "GCUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    from pastis_gb300 import capi, synth
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    mode = capi.MODE_SW if args.workload == "sw100k" else capi.MODE_XDROP
+    # weak scaling: every rank aligns its own batch of the same shape
+    w = synth.generate(args.workload, seed=20260101 + rank, scale=args.scale)
+    n = len(w.pairs)
+    cfg = capi.config(mode, device=dev)
+    ctx = capi.Context(cfg)
+    ctx.set_seqs(0, w.ascii, w.offs)
+    ctx.share_row_seqs()
+
+    stream = torch.cuda.current_stream(dev)
+    d_pairs = torch.from_numpy(w.pairs.view(np.uint8).copy()).to(f"cuda:{dev}")
+    d_out = torch.empty(n * capi.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{dev}")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+
+    def step():
+        ctx.align_device(d_pairs.data_ptr(), n, d_out.data_ptr(), stream.cuda_stream)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize(dev)
+    res = np.frombuffer(d_out.cpu().numpy().tobytes(), dtype=capi.RESULT_DTYPE)
+    alg_cells = int(res["cells"].astype(np.uint64).sum())
+
+    clocks = Clocks(dev)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    exec0 = ctx.exec_cells()
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    t_wall = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)          # evict the previous step's working set from L2
+        ev[k][0].record(stream)
+        step()
+        ev[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    t_wall = time.perf_counter() - t_wall
+    if dist is not None:
+        dist.barrier()
+    clk = clocks.stop()
+    launches = ctx.last_launches() * args.steps
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    exec_cells = (ctx.exec_cells() - exec0) / args.steps
+    if dist is not None:
+        t = torch.tensor([total_ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    gcups = alg_cells * world / (ms_step * 1e-3) / 1e9
+    aln_s = n * world / (ms_step * 1e-3)
+
+    # end to end: pinned host pairs in, results out, through pg_align
+    h_pairs = torch.empty(n * capi.PAIR_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
+    h_pairs.numpy()[:] = w.pairs.view(np.uint8)
+    h_out = torch.empty(n * capi.RESULT_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
+    pv = h_pairs.numpy().view(capi.PAIR_DTYPE)
+    ov = h_out.numpy().view(capi.RESULT_DTYPE)
+    ctx.align(pv, out=ov)
+    e2e_t = []
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)
+        torch.cuda.synchronize(dev)
+        if dist is not None:
+            dist.barrier()
+        t0 = time.perf_counter()
+        ctx.align(pv, out=ov)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e_t)
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=f"cuda:{dev}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_gcups = alg_cells * world / e2e_s / 1e9
+    same = bool((ov.view(np.uint8) == res.view(np.uint8)).all())
+
+    line = None
+    if rank == 0:
+        peak_ops = capi.dpx_peak(dev)
+        peak_gcups = peak_ops / DPX_OPS_PER_CELL / 1e9
+        achieved = exec_cells / (ms_step * 1e-3) / 1e9
+        traffic = None
+        tpath = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tpath):
+            tr = json.load(open(tpath)).get(args.workload)
+            if tr and tr.get("bytes_per_pair"):
+                traffic = tr["bytes_per_pair"] * n
+        peaks = {}
+        ppath = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(ppath):
+            peaks = json.load(open(ppath))
+        lens = w.lengths()
+        alg_bytes = int((lens[w.pairs["row"]] + lens[w.pairs["col"]]).sum()) + n * (
+            capi.PAIR_DTYPE.itemsize + capi.RESULT_DTYPE.itemsize)
+        hbm_gbs = alg_bytes / (ms_step * 1e-3) / 1e9
+        line = {
+            "metric": METRIC, "value": gcups, "unit": "GCUPS", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32", "data": "synthetic",
+            "config": {"workload": args.workload + ": " + workload_desc(args.workload, n,
+                                                                        args.scale),
+                       "mode": "xdrop" if mode else "sw", "pairs": n,
+                       "scoring": "BLOSUM62; gap_open -11, gap_ext -2 given to the score "
+                                  "model in SeqAn's constructor order, as PASTIS calls it",
+                       "l2": "flushed between timed steps (512 MiB write, outside the "
+                             "timed region)",
+                       "parallelism": "dp%d (independent pair batches per GPU)" % world},
+            "alignments_per_s": aln_s,
+            "algorithmic_cells_per_step": alg_cells,
+            "executed_cells_per_step": exec_cells,
+            "gpu_launches": launches,
+            "clocks": clk,
+            "e2e": {"value": e2e_gcups, "unit": "GCUPS",
+                    "alignments_per_s": n * world / e2e_s,
+                    "h2d_bytes_per_step": n * capi.PAIR_DTYPE.itemsize,
+                    "d2h_bytes_per_step": n * capi.RESULT_DTYPE.itemsize,
+                    "matches_device_run": same},
+            "roofline": {"bound": "dpx", "achieved": achieved, "peak": peak_gcups,
+                         "unit": "GCUPS", "frac": achieved / peak_gcups, "traffic": traffic,
+                         "kernel": "k_xdrop" if mode else "k_sw",
+                         "peak_source": "measured %.4g DPX add-max/s (pg_dpx_peak) / %d "
+                                        "int32 DPX ops per cell" % (peak_ops, DPX_OPS_PER_CELL),
+                         "hbm": {"achieved_GBps": hbm_gbs,
+                                 "peak_GBps": peaks.get("hbm_gbs"),
+                                 "frac": hbm_gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs")
+                                 else None,
+                                 "note": "algorithmic bytes: residues of both sequences, "
+                                         "the pair record and the result per pair"}},
+            "wall_s_timed": t_wall,
+        }
+    if not args.no_cpu_baseline and rank == 0:
+        cores = host_cores()
+        p = oracle_params(cfg)
+        cells, ns, dt = cpu_sample(w, mode, p, args.cpu_seconds, cores)
+        line["cpu_baseline"] = {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": cores,
+                                "kind": "port",
+                                "sample": "first %d of %d pairs (%.3g cells) in %.1f s" % (
+                                    ns, n, cells, dt),
+                                "alignments_per_s": ns / dt}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    from pastis_gb300 import build
+    build.build()
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        run_gpu(args, rank, world, local_rank)
+
+
+import numpy as np  # noqa: E402
+
+if __name__ == "__main__":
+    main()

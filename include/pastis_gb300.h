@@ -1,0 +1,164 @@
+/*
+ * pastis_gb300.h -- C ABI of the GB300 batched pairwise aligner for PASTIS.
+ *
+ * Drop-in for the arithmetic behind PASTIS's aligner plug-in interface
+ * (inc/align/PWAlign.hpp:20-82).  A PWAlign subclass on the host:
+ *   construct_seqs / construct_seqs_bl (PWAlign.hpp:33-41)  -> pg_set_seqs
+ *   aln_batch(tuples, beg, end, roff, coff, params)          -> pg_align
+ *     replacing seqan::localAlignment      (src/align/SeqanFullAligner.cpp:231)
+ *     and seqan::extendSeed + globalAlignment
+ *                                         (src/align/SeqanXdropAligner.cpp:281-296)
+ *     and computeAlignmentStats + the coverage/ANI filter
+ *                                         (SeqanFullAligner.cpp:238-263,
+ *                                          SeqanXdropAligner.cpp:303-354)
+ * Plain C types only; no exceptions cross the ABI.  Every call returns 0 or a
+ * negative PG_ERR_* code; pg_strerror names it and pg_last_error gives detail.
+ * One context per host thread (a context is not thread-safe).
+ */
+#ifndef PASTIS_GB300_H
+#define PASTIS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes */
+#define PG_OK            0
+#define PG_ERR_ARG      -1   /* bad argument (null pointer, size, index, option) */
+#define PG_ERR_CUDA     -2   /* a CUDA runtime call failed */
+#define PG_ERR_OOM      -3   /* device or pinned-host allocation failed */
+#define PG_ERR_TIMEOUT  -4   /* a bounded device wait ran out (status word set) */
+#define PG_ERR_STATE    -5   /* call order (e.g. pg_align before pg_set_seqs) */
+#define PG_ERR_RANGE    -6   /* a sequence is longer than 65535 residues */
+#define PG_ERR_NODEV    -7   /* no CUDA device / device id out of range */
+
+/* ---- alignment modes (params_t::PwAln, inc/Types.hpp:52-59) */
+#define PG_MODE_SW     0     /* --sfa: affine local alignment (ALN_SEQAN_FULL)  */
+#define PG_MODE_XDROP  1     /* --sxa: seeded X-drop + global (ALN_SEQAN_XDROP) */
+
+/* ---- how PASTIS's (gap_open, gap_ext) reach the score model.
+ * PASTIS constructs seqan::Blosum62(gap_open, gap_ext)
+ * (inc/align/SeqanFullAligner.hpp:35-38, SeqanXdropAligner.hpp:38-43); SeqAn's
+ * two-argument Score constructor takes (gapExtend, gapOpen).  PG_GAPS_AS_CALLED
+ * reproduces that (first gap position scores gap_ext, further positions
+ * gap_open, X-drop uses gap_open); PG_GAPS_NOMINAL uses the parameters by name
+ * (first position gap_open, further gap_ext, X-drop gap_ext). */
+#define PG_GAPS_AS_CALLED 0
+#define PG_GAPS_NOMINAL   1
+
+/* ---- traceback tie-breaking (the choices SeqAn's traceback makes on ties) */
+#define PG_TIE_H_E_BEFORE_F   1   /* H ties: diag > horizontal > vertical (default diag > vertical > horizontal) */
+#define PG_TIE_GAP_OPEN_FIRST 2   /* gap ties: open > extend (default extend > open) */
+
+/* ---- behaviour flags */
+#define PG_F_SKIP_SPURIOUS_SEED 1 /* skip the (0,0) second seed of count==1 pairs
+                                     (the reference extends it: SeqanXdropAligner.cpp:273-277) */
+
+/* ---- per-pair result flags */
+#define PG_RF_EMPTY     1   /* no alignment columns (identity reported as 0) */
+#define PG_RF_BAD_SEED  2   /* a seed ran past a sequence end and was clamped */
+#define PG_RF_PASSED    4   /* coverage/ANI filter passed, score_aln = identity/100 */
+
+#define PG_NRES 25          /* residue codes, order ARNDCQEGHILKMFPSTWYVBZX*J */
+
+typedef struct pg_config {
+    int32_t mode;           /* PG_MODE_* */
+    int32_t gap_open;       /* params_t::gap_open (default -11, src/main.cpp:158-161) */
+    int32_t gap_ext;        /* params_t::gap_ext  (default -2,  src/main.cpp:163-166) */
+    int32_t gap_semantics;  /* PG_GAPS_* */
+    int32_t xdrop;          /* params_t::aln_seqan_xdrop (--sxa value) */
+    int32_t seed_len;       /* params_t::klength (default 6) */
+    int32_t seed_count;     /* params_t::seed_count (default 2) */
+    int32_t tie;            /* PG_TIE_* */
+    int32_t flags;          /* PG_F_* */
+    int32_t ani_thr;        /* params_t::aln_ani_thr (30) */
+    double  cov_thr;        /* params_t::aln_cov_thr (0.7) */
+    int32_t device;         /* CUDA device ordinal */
+    int32_t reserved;
+    const int8_t *score_matrix; /* PG_NRES x PG_NRES row-major, or NULL for BLOSUM62 */
+} pg_config;
+
+/* One candidate pair = one tuple of pw_aln_batch (src/DistPWRunner.cpp:100-102):
+ * local row / column index plus the CommonKmerLoc fields the aligner reads
+ * (inc/Types.hpp:166-171): count, score, first = (rs0, cs0), second = (rs1, cs1). */
+typedef struct pg_pair {
+    uint32_t row, col;
+    uint16_t rs0, cs0, rs1, cs1;
+    uint16_t count;
+    int16_t  score;
+} pg_pair;
+
+/* Per-pair result.  H = column sequence, V = row sequence; coordinates are
+ * 0-based half-open residue ranges of the aligned region. */
+typedef struct pg_result {
+    int32_t  score;         /* SW: local score; X-drop: global score of the kept seed */
+    uint32_t aln_len;       /* alignment columns */
+    uint32_t matches;       /* identical columns */
+    uint32_t gap_opens;     /* gap runs, counted per row */
+    uint16_t beg_h, end_h, beg_v, end_v;
+    float    identity;      /* (float)(100.0 * matches / aln_len) */
+    float    score_aln;     /* identity/100 if the coverage/ANI filter passes, else 0 */
+    uint8_t  seed_used;     /* X-drop: which seed was kept (0 or 1) */
+    uint8_t  flags;         /* PG_RF_* */
+    uint16_t pad;
+    uint32_t cells;         /* algorithmic DP cells of this pair (saturating) */
+} pg_result;
+
+typedef struct pg_ctx pg_ctx;
+
+/* Fill cfg with PASTIS's defaults for a mode (src/main.cpp:97-116, :153-176). */
+void pg_config_default(pg_config *cfg, int32_t mode);
+
+int  pg_create(const pg_config *cfg, pg_ctx **out);
+void pg_destroy(pg_ctx *ctx);
+
+/* Load the row (side 0) or column (side 1) sequences of this rank's block:
+ * ASCII residues concatenated, offsets[0..n] (offsets[n] = total bytes).  Lower
+ * case is folded, letters outside ARNDCQEGHILKMFPSTWYVBZX*J score as X.
+ * Replaces construct_seqs / construct_seqs_bl (PWAlign.hpp:33-41). */
+int pg_set_seqs(pg_ctx *ctx, int32_t side, const char *residues,
+                const uint64_t *offsets, uint64_t n);
+/* Use the row sequences for the columns too (diagonal grid cell,
+ * SeqanFullAligner.cpp:82-87). */
+int pg_share_row_seqs(pg_ctx *ctx);
+
+/* Align n pairs in host memory; writes n results to host memory.  Pair i uses
+ * row sequence pairs[i].row + bl_roffset and column sequence
+ * pairs[i].col + bl_coffset (PWAlign::aln_batch, PWAlign.hpp:47-63).  n == 0
+ * is a no-op.  Synchronous. */
+int pg_align(pg_ctx *ctx, const pg_pair *pairs, uint64_t n,
+             uint64_t bl_roffset, uint64_t bl_coffset, pg_result *out);
+
+/* Same, on device buffers, enqueued on `stream` (a cudaStream_t, NULL = the
+ * context's stream); returns after enqueueing.  Call pg_sync (or synchronize
+ * the stream) before reading `out`. */
+int pg_align_device(pg_ctx *ctx, const pg_pair *d_pairs, uint64_t n,
+                    uint64_t bl_roffset, uint64_t bl_coffset, pg_result *d_out,
+                    void *stream);
+int pg_sync(pg_ctx *ctx);
+
+/* Number of kernel launches made by the last pg_align / pg_align_device call. */
+int pg_last_launches(const pg_ctx *ctx);
+
+/* DP cells the kernels actually computed since pg_create (synchronizing read).
+ * Differs from the sum of pg_result::cells where the kernel skips a second
+ * seed whose extension or alignment repeats the first one's. */
+unsigned long long pg_exec_cells(pg_ctx *ctx);
+
+/* Measured throughput of the DPX add-max instruction on a device, in
+ * instructions per second over all SMs (the roofline of the DP kernels). */
+int pg_dpx_peak(int device, double *ops_per_s);
+
+const char *pg_strerror(int code);
+const char *pg_last_error(void);
+
+/* Library version string and the device architecture it was compiled for. */
+const char *pg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

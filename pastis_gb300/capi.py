@@ -1,0 +1,265 @@
+"""ctypes bindings of the C ABI (include/pastis_gb300.h) and the C++ host driver.
+
+The CUDA library must be present: loading raises if it is missing, there is no
+CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+BUILD = _build.BUILD
+
+PG_OK = 0
+PG_ERR_ARG, PG_ERR_CUDA, PG_ERR_OOM, PG_ERR_TIMEOUT = -1, -2, -3, -4
+PG_ERR_STATE, PG_ERR_RANGE, PG_ERR_NODEV = -5, -6, -7
+MODE_SW, MODE_XDROP = 0, 1
+GAPS_AS_CALLED, GAPS_NOMINAL = 0, 1
+TIE_H_E_BEFORE_F, TIE_GAP_OPEN_FIRST = 1, 2
+F_SKIP_SPURIOUS_SEED = 1
+RF_EMPTY, RF_BAD_SEED, RF_PASSED = 1, 2, 4
+NRES = 25
+LETTERS = "ARNDCQEGHILKMFPSTWYVBZX*J"
+
+PAIR_DTYPE = np.dtype([("row", "<u4"), ("col", "<u4"), ("rs0", "<u2"), ("cs0", "<u2"),
+                       ("rs1", "<u2"), ("cs1", "<u2"), ("count", "<u2"), ("score", "<i2")])
+RESULT_DTYPE = np.dtype([("score", "<i4"), ("aln_len", "<u4"), ("matches", "<u4"),
+                         ("gap_opens", "<u4"), ("beg_h", "<u2"), ("end_h", "<u2"),
+                         ("beg_v", "<u2"), ("end_v", "<u2"), ("identity", "<f4"),
+                         ("score_aln", "<f4"), ("seed_used", "u1"), ("flags", "u1"),
+                         ("pad", "<u2"), ("cells", "<u4")])
+# inc/Types.hpp CommonKmerLoc (16 B) and CommonKmerLight (8 B)
+KMERLOC_DTYPE = np.dtype([("count", "<u2"), ("score", "<i2"), ("score_aln", "<f4"),
+                          ("first_r", "<u2"), ("first_c", "<u2"),
+                          ("second_r", "<u2"), ("second_c", "<u2")])
+KMERLIGHT_DTYPE = np.dtype([("count", "<u2"), ("score", "<i2"), ("score_aln", "<f4")])
+assert PAIR_DTYPE.itemsize == 20 and RESULT_DTYPE.itemsize == 40
+assert KMERLOC_DTYPE.itemsize == 16 and KMERLIGHT_DTYPE.itemsize == 8
+
+# every entry point declared in include/*.h (checked by the CPU tests)
+EXPORTS = {
+    "libpastis_gb300.so": ["pg_config_default", "pg_create", "pg_destroy", "pg_set_seqs",
+                           "pg_share_row_seqs", "pg_align", "pg_align_device", "pg_sync",
+                           "pg_last_launches", "pg_exec_cells", "pg_dpx_peak", "pg_strerror", "pg_last_error",
+                           "pg_version"],
+    "libpastis_synth.so": ["pg_synth_generate", "pg_synth_free", "pg_synth_nseqs",
+                           "pg_synth_nres", "pg_synth_npairs", "pg_synth_seq", "pg_synth_offs",
+                           "pg_synth_family", "pg_synth_pairs", "pg_synth_homolog",
+                           "pg_synth_spurious"],
+    "libpastis_host.so": ["pgh_pw_aln_batch", "pgh_last_error"],
+}
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int32), ("gap_open", ctypes.c_int32),
+                ("gap_ext", ctypes.c_int32), ("gap_semantics", ctypes.c_int32),
+                ("xdrop", ctypes.c_int32), ("seed_len", ctypes.c_int32),
+                ("seed_count", ctypes.c_int32), ("tie", ctypes.c_int32),
+                ("flags", ctypes.c_int32), ("ani_thr", ctypes.c_int32),
+                ("cov_thr", ctypes.c_double), ("device", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("score_matrix", ctypes.c_void_p)]
+
+
+_libs = {}
+
+
+def load(name="libpastis_gb300.so"):
+    """Load one of the native libraries (built in-tree by pastis_gb300.build)."""
+    if name not in _libs:
+        path = os.path.join(BUILD, name)
+        if not os.path.exists(path):
+            raise RuntimeError("native library %s is missing; run pastis_gb300.build.build()" % path)
+        lib = ctypes.CDLL(path, mode=ctypes.RTLD_GLOBAL)
+        _declare(name, lib)
+        _libs[name] = lib
+    return _libs[name]
+
+
+def _declare(name, lib):
+    vp, u64, i32 = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32
+    if name == "libpastis_gb300.so":
+        lib.pg_config_default.argtypes = [ctypes.POINTER(Config), i32]
+        lib.pg_config_default.restype = None
+        lib.pg_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(vp)]
+        lib.pg_destroy.argtypes = [vp]
+        lib.pg_destroy.restype = None
+        lib.pg_set_seqs.argtypes = [vp, i32, vp, vp, u64]
+        lib.pg_share_row_seqs.argtypes = [vp]
+        lib.pg_align.argtypes = [vp, vp, u64, u64, u64, vp]
+        lib.pg_align_device.argtypes = [vp, vp, u64, u64, u64, vp, vp]
+        lib.pg_sync.argtypes = [vp]
+        lib.pg_last_launches.argtypes = [vp]
+        lib.pg_exec_cells.argtypes = [vp]
+        lib.pg_exec_cells.restype = ctypes.c_ulonglong
+        lib.pg_dpx_peak.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
+        lib.pg_strerror.argtypes = [i32]
+        lib.pg_strerror.restype = ctypes.c_char_p
+        lib.pg_last_error.restype = ctypes.c_char_p
+        lib.pg_version.restype = ctypes.c_char_p
+    elif name == "libpastis_synth.so":
+        lib.pg_synth_generate.argtypes = [vp]
+        lib.pg_synth_generate.restype = vp
+        for f in ("pg_synth_nseqs", "pg_synth_nres", "pg_synth_npairs"):
+            getattr(lib, f).argtypes = [vp]
+            getattr(lib, f).restype = u64
+        for f in ("pg_synth_seq", "pg_synth_offs", "pg_synth_family", "pg_synth_pairs",
+                  "pg_synth_homolog", "pg_synth_spurious"):
+            getattr(lib, f).argtypes = [vp]
+            getattr(lib, f).restype = vp
+        lib.pg_synth_free.argtypes = [vp]
+        lib.pg_synth_free.restype = None
+    elif name == "libpastis_host.so":
+        lib.pgh_last_error.restype = ctypes.c_char_p
+
+
+class PgError(RuntimeError):
+    def __init__(self, code, detail=""):
+        self.code = code
+        msg = load().pg_strerror(code).decode()
+        super().__init__("%s (%d): %s" % (msg, code, detail))
+
+
+def _check(rc):
+    if rc != PG_OK:
+        raise PgError(rc, load().pg_last_error().decode(errors="replace"))
+
+
+def config(mode=MODE_XDROP, **kw):
+    c = Config()
+    load().pg_config_default(ctypes.byref(c), mode)
+    for k, v in kw.items():
+        if k == "score_matrix":
+            continue
+        setattr(c, k, v)
+    return c
+
+
+def resolved_gaps(cfg):
+    """(first position, further positions, X-drop linear gap) the kernels use."""
+    if cfg.gap_semantics == GAPS_AS_CALLED:
+        return cfg.gap_ext, cfg.gap_open, cfg.gap_open
+    return cfg.gap_open, cfg.gap_ext, cfg.gap_ext
+
+
+def dpx_peak(device=0):
+    """Measured DPX add-max instructions per second on a device."""
+    v = ctypes.c_double()
+    _check(load().pg_dpx_peak(device, ctypes.byref(v)))
+    return v.value
+
+
+def decode(codes):
+    lut = np.frombuffer(LETTERS.encode(), dtype=np.uint8)
+    return lut[np.asarray(codes, dtype=np.uint8)]
+
+
+class Context:
+    """Owns one pg_ctx (one device, one mode)."""
+
+    def __init__(self, cfg):
+        self.lib = load()
+        self.cfg = cfg
+        self._sm = None
+        h = ctypes.c_void_p()
+        _check(self.lib.pg_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_seqs(self, side, residues_ascii, offsets):
+        res = np.ascontiguousarray(residues_ascii, dtype=np.uint8)
+        offs = np.ascontiguousarray(offsets, dtype=np.uint64)
+        _check(self.lib.pg_set_seqs(self.h, side, res.ctypes.data, offs.ctypes.data,
+                                    len(offs) - 1))
+
+    def share_row_seqs(self):
+        _check(self.lib.pg_share_row_seqs(self.h))
+
+    def align(self, pairs, bl_roff=0, bl_coff=0, out=None):
+        pairs = np.ascontiguousarray(pairs, dtype=PAIR_DTYPE)
+        if out is None:
+            out = np.zeros(len(pairs), dtype=RESULT_DTYPE)
+        _check(self.lib.pg_align(self.h, pairs.ctypes.data, len(pairs), bl_roff, bl_coff,
+                                 out.ctypes.data))
+        return out
+
+    def align_device(self, d_pairs_ptr, n, d_out_ptr, stream_ptr=None, bl_roff=0, bl_coff=0):
+        _check(self.lib.pg_align_device(self.h, d_pairs_ptr, n, bl_roff, bl_coff, d_out_ptr,
+                                        stream_ptr))
+
+    def sync(self):
+        _check(self.lib.pg_sync(self.h))
+
+    def last_launches(self):
+        return int(self.lib.pg_last_launches(self.h))
+
+    def exec_cells(self):
+        return int(self.lib.pg_exec_cells(self.h))
+
+
+ALIGN_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
+                            ctypes.c_uint64, ctypes.POINTER(ctypes.c_float), ctypes.c_void_p)
+
+
+def pw_aln_batch(mode, rows, cols, vals, row_res, row_offs, col_res=None, col_offs=None,
+                 bl_roff=0, bl_coff=0, batch_sz=10 ** 10, ckthr=0, mosthr=-1.0, cfg=None,
+                 callback=None):
+    """Run the C++ pw_aln_batch driver (src/DistPWRunner.cpp:25-165) on one block.
+
+    vals is a KMERLOC_DTYPE (X-drop) or KMERLIGHT_DTYPE (SW) array.  With
+    ``callback(pairs, bl_roff, bl_coff) -> score_aln array`` the driver uses it
+    as the aligner instead of the GPU.  Returns (rows, cols, vals, stats)."""
+    lib = load("libpastis_host.so")
+    rows = np.array(rows, dtype=np.uint64)
+    cols = np.array(cols, dtype=np.uint64)
+    vals = np.array(vals, dtype=KMERLOC_DTYPE if mode == MODE_XDROP else KMERLIGHT_DTYPE)
+    rres = np.ascontiguousarray(row_res, dtype=np.uint8)
+    roffs = np.ascontiguousarray(row_offs, dtype=np.uint64)
+    if col_res is not None:
+        cres = np.ascontiguousarray(col_res, dtype=np.uint8)
+        coffs = np.ascontiguousarray(col_offs, dtype=np.uint64)
+        cres_p, coffs_p, nc = cres.ctypes.data, coffs.ctypes.data, len(coffs) - 1
+    else:
+        cres_p, coffs_p, nc = None, None, 0
+    stats = np.zeros(5, dtype=np.uint64)
+    secs = np.zeros(4, dtype=np.float64)
+    cb = None
+    if callback is not None:
+        def _cb(pp, n, ro, co, out, user):
+            try:
+                arr = np.ctypeslib.as_array((ctypes.c_char * (n * PAIR_DTYPE.itemsize))
+                                            .from_address(pp)).view(PAIR_DTYPE).copy()
+                s = np.ascontiguousarray(callback(arr, ro, co), dtype=np.float32)
+                ctypes.memmove(out, s.ctypes.data, 4 * n)
+                return 0
+            except Exception:
+                return 1
+        cb = ALIGN_CB(_cb)
+    c = cfg if cfg is not None else config(mode)
+    vp, u64 = ctypes.c_void_p, ctypes.c_uint64
+    rc = lib.pgh_pw_aln_batch(ctypes.c_int(mode), ctypes.byref(c), vp(rres.ctypes.data),
+                              vp(roffs.ctypes.data), u64(len(roffs) - 1), vp(cres_p),
+                              vp(coffs_p), u64(nc), u64(len(vals)), vp(rows.ctypes.data),
+                              vp(cols.ctypes.data), vp(vals.ctypes.data), u64(bl_roff),
+                              u64(bl_coff), u64(batch_sz), ctypes.c_int(ckthr),
+                              ctypes.c_float(mosthr), cb, None, vp(stats.ctypes.data),
+                              vp(secs.ctypes.data))
+    if rc != PG_OK:
+        raise RuntimeError("pw_aln_batch failed (%d): %s" % (rc, lib.pgh_last_error().decode()))
+    k = int(stats[2])
+    return rows[:k], cols[:k], vals[:k], {
+        "nnz_in": int(stats[0]), "nnz_kmer_thr": int(stats[1]), "nnz_aln": int(stats[2]),
+        "batches": int(stats[3]), "empty_batches": int(stats[4]),
+        "seconds": {"align|pre": secs[0], "align|gpu": secs[1], "align|post": secs[2],
+                    "align": secs[3]}}

@@ -1,0 +1,160 @@
+// host.cpp -- C entry points over the C++ host side (pastis_gb300_pwalign.hpp),
+// so that the batch driver can be exercised from any language.
+//
+// pgh_pw_aln_batch runs pw_aln_batch (src/DistPWRunner.cpp:25-165) on one
+// rank's block with either the GPU aligner or a caller-supplied aligner
+// callback (used to test the driver's pruning and batching without a GPU).
+#include <cstring>
+#include <exception>
+#include <string>
+
+#include "pastis_gb300.h"
+#include "pastis_gb300_pwalign.hpp"
+
+extern "C" {
+
+// callback aligner: fills score_aln[i] for pairs[0..n)
+typedef int (*pgh_align_cb)(const pg_pair *pairs, uint64_t n, uint64_t bl_roff, uint64_t bl_coff,
+                            float *score_aln, void *user);
+
+int pgh_pw_aln_batch(int mode, const pg_config *cfg,
+                     const char *rres, const uint64_t *roffs, uint64_t nr,
+                     const char *cres, const uint64_t *coffs, uint64_t nc,
+                     uint64_t nnz, uint64_t *rows, uint64_t *cols, void *vals,
+                     uint64_t bl_roff, uint64_t bl_coff, uint64_t batch_sz, int ckthr, float mosthr,
+                     pgh_align_cb cb, void *cb_user, uint64_t *out_stats, double *out_seconds);
+}
+
+namespace {
+
+thread_local std::string g_host_err;
+
+class CallbackAligner : public pastis::PWAlign {
+public:
+    CallbackAligner(pgh_align_cb cb, void *user) : cb_(cb), user_(user) {}
+    void construct_seqs(const pastis::SeqSet &, const pastis::SeqSet &) override {}
+    void construct_seqs_bl(const pastis::SeqSet &) override {}
+    void aln_batch(std::tuple<uint64_t, uint64_t, pastis::CommonKmerLight *> *t, uint64_t beg,
+                   uint64_t end, uint64_t ro, uint64_t co, const pastis::params_t &) override
+    {
+        run(t, beg, end, ro, co);
+    }
+    void aln_batch(std::tuple<uint64_t, uint64_t, pastis::CommonKmerLoc *> *t, uint64_t beg,
+                   uint64_t end, uint64_t ro, uint64_t co, const pastis::params_t &) override
+    {
+        run(t, beg, end, ro, co);
+    }
+    uint64_t calls = 0, empty_calls = 0;
+
+private:
+    pgh_align_cb cb_;
+    void *user_;
+    static void seeds(pg_pair &p, const pastis::CommonKmerLight *) { p.rs0 = p.cs0 = p.rs1 = p.cs1 = 0; }
+    static void seeds(pg_pair &p, const pastis::CommonKmerLoc *v)
+    {
+        p.rs0 = v->first.first; p.cs0 = v->first.second;
+        p.rs1 = v->second.first; p.cs1 = v->second.second;
+    }
+    template <typename NT>
+    void run(std::tuple<uint64_t, uint64_t, NT *> *t, uint64_t beg, uint64_t end, uint64_t ro, uint64_t co)
+    {
+        ++calls;
+        if (end <= beg) { ++empty_calls; return; }
+        std::vector<pg_pair> p(end - beg);
+        std::vector<float> s(end - beg, 0.0f);
+        for (uint64_t i = beg; i < end; ++i) {
+            pg_pair &q = p[i - beg];
+            q.row = (uint32_t)std::get<0>(t[i]);
+            q.col = (uint32_t)std::get<1>(t[i]);
+            q.count = std::get<2>(t[i])->count;
+            q.score = std::get<2>(t[i])->score;
+            seeds(q, std::get<2>(t[i]));
+        }
+        if (cb_(p.data(), end - beg, ro, co, s.data(), user_) != 0)
+            throw std::runtime_error("aligner callback failed");
+        for (uint64_t i = beg; i < end; ++i) std::get<2>(t[i])->score_aln = s[i - beg];
+    }
+};
+
+template <typename NT>
+int drive(int mode, const pg_config *cfg, const char *rres, const uint64_t *roffs, uint64_t nr,
+          const char *cres, const uint64_t *coffs, uint64_t nc, uint64_t nnz, uint64_t *rows,
+          uint64_t *cols, NT *vals, uint64_t bl_roff, uint64_t bl_coff, uint64_t batch_sz, int ckthr,
+          float mosthr, pgh_align_cb cb, void *cb_user, uint64_t *out_stats, double *out_seconds)
+{
+    pastis::params_t params;
+    params.aln_batch_sz = batch_sz;
+    params.ckthr = ckthr;
+    params.mosthr = mosthr;
+    pastis::LocalMat<NT> C;
+    C.row.assign(rows, rows + nnz);
+    C.col.assign(cols, cols + nnz);
+    C.val.assign(vals, vals + nnz);
+    pastis::BatchStats st;
+    std::unique_ptr<pastis::PWAlign> pwa;
+    if (cb) {
+        pwa.reset(new CallbackAligner(cb, cb_user));
+    } else {
+        if (!cfg) return PG_ERR_ARG;
+        if (mode == PG_MODE_XDROP)
+            pwa.reset(new pastis::GpuAligner(cfg->gap_open, cfg->gap_ext, (pastis::ushort)cfg->seed_len,
+                                             cfg->xdrop, cfg->seed_count, cfg->device,
+                                             cfg->gap_semantics, cfg->tie, cfg->flags));
+        else
+            pwa.reset(new pastis::GpuAligner(cfg->gap_open, cfg->gap_ext, cfg->device,
+                                             cfg->gap_semantics, cfg->tie, cfg->flags));
+        pastis::SeqSet R, Cs;
+        R.residues = rres;
+        R.offsets.assign(roffs, roffs + nr + 1);
+        if (cres) {
+            Cs.residues = cres;
+            Cs.offsets.assign(coffs, coffs + nc + 1);
+            pwa->construct_seqs(R, Cs);
+        } else {
+            pwa->construct_seqs_bl(R);
+        }
+    }
+    st = pastis::pw_aln_batch(C, *pwa, params, bl_roff, bl_coff);
+    for (uint64_t i = 0; i < C.nnz(); ++i) { rows[i] = C.row[i]; cols[i] = C.col[i]; vals[i] = C.val[i]; }
+    if (out_stats) {
+        out_stats[0] = st.nnz_in; out_stats[1] = st.nnz_kmer_thr; out_stats[2] = st.nnz_aln;
+        out_stats[3] = st.batches;
+        CallbackAligner *ca = dynamic_cast<CallbackAligner *>(pwa.get());
+        out_stats[4] = ca ? ca->empty_calls : 0;
+    }
+    if (out_seconds) {
+        out_seconds[0] = pwa->tp.seconds["align|pre"];
+        out_seconds[1] = pwa->tp.seconds["align|gpu"];
+        out_seconds[2] = pwa->tp.seconds["align|post"];
+        out_seconds[3] = pwa->tp.seconds["align"];
+    }
+    return PG_OK;
+}
+
+}  // namespace
+
+extern "C" int pgh_pw_aln_batch(int mode, const pg_config *cfg,
+                                const char *rres, const uint64_t *roffs, uint64_t nr,
+                                const char *cres, const uint64_t *coffs, uint64_t nc,
+                                uint64_t nnz, uint64_t *rows, uint64_t *cols, void *vals,
+                                uint64_t bl_roff, uint64_t bl_coff, uint64_t batch_sz, int ckthr,
+                                float mosthr, pgh_align_cb cb, void *cb_user, uint64_t *out_stats,
+                                double *out_seconds)
+{
+    try {
+        if (mode == PG_MODE_XDROP)
+            return drive(mode, cfg, rres, roffs, nr, cres, coffs, nc, nnz, rows, cols,
+                         (pastis::CommonKmerLoc *)vals, bl_roff, bl_coff, batch_sz, ckthr, mosthr,
+                         cb, cb_user, out_stats, out_seconds);
+        if (mode == PG_MODE_SW)
+            return drive(mode, cfg, rres, roffs, nr, cres, coffs, nc, nnz, rows, cols,
+                         (pastis::CommonKmerLight *)vals, bl_roff, bl_coff, batch_sz, ckthr, mosthr,
+                         cb, cb_user, out_stats, out_seconds);
+        return PG_ERR_ARG;
+    } catch (const std::exception &e) {
+        g_host_err = e.what();
+        return PG_ERR_STATE;
+    }
+}
+
+extern "C" const char *pgh_last_error(void) { return g_host_err.c_str(); }

@@ -1,0 +1,500 @@
+// pg_api.cu -- C ABI of the GB300 batched pairwise aligner (declared in
+// include/pastis_gb300.h).  Host side: sequence residency, scratch sizing,
+// launch of the persistent kernels in pg_kernels.cuh, error reporting.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include "../../include/pastis_gb300.h"
+#include "pg_kernels.cuh"
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+int fail(int code, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CU(call)                                                                   \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess)                                                     \
+            return fail(e_ == cudaErrorMemoryAllocation ? PG_ERR_OOM : PG_ERR_CUDA, \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                 \
+    } while (0)
+
+// Published BLOSUM62 in PASTIS's residue order ARNDCQEGHILKMFPSTWYVBZX*J
+// (src/Alphabet.cpp:26); J scores as L, as in inc/ScoreMat.hpp:104-131.
+const signed char kB62[24][24] = {
+    { 4,-1,-2,-2, 0,-1,-1, 0,-2,-1,-1,-1,-1,-2,-1, 1, 0,-3,-2, 0,-2,-1, 0,-4},
+    {-1, 5, 0,-2,-3, 1, 0,-2, 0,-3,-2, 2,-1,-3,-2,-1,-1,-3,-2,-3,-1, 0,-1,-4},
+    {-2, 0, 6, 1,-3, 0, 0, 0, 1,-3,-3, 0,-2,-3,-2, 1, 0,-4,-2,-3, 3, 0,-1,-4},
+    {-2,-2, 1, 6,-3, 0, 2,-1,-1,-3,-4,-1,-3,-3,-1, 0,-1,-4,-3,-3, 4, 1,-1,-4},
+    { 0,-3,-3,-3, 9,-3,-4,-3,-3,-1,-1,-3,-1,-2,-3,-1,-1,-2,-2,-1,-3,-3,-2,-4},
+    {-1, 1, 0, 0,-3, 5, 2,-2, 0,-3,-2, 1, 0,-3,-1, 0,-1,-2,-1,-2, 0, 3,-1,-4},
+    {-1, 0, 0, 2,-4, 2, 5,-2, 0,-3,-3, 1,-2,-3,-1, 0,-1,-3,-2,-2, 1, 4,-1,-4},
+    { 0,-2, 0,-1,-3,-2,-2, 6,-2,-4,-4,-2,-3,-3,-2, 0,-2,-2,-3,-3,-1,-2,-1,-4},
+    {-2, 0, 1,-1,-3, 0, 0,-2, 8,-3,-3,-1,-2,-1,-2,-1,-2,-2, 2,-3, 0, 0,-1,-4},
+    {-1,-3,-3,-3,-1,-3,-3,-4,-3, 4, 2,-3, 1, 0,-3,-2,-1,-3,-1, 3,-3,-3,-1,-4},
+    {-1,-2,-3,-4,-1,-2,-3,-4,-3, 2, 4,-2, 2, 0,-3,-2,-1,-2,-1, 1,-4,-3,-1,-4},
+    {-1, 2, 0,-1,-3, 1, 1,-2,-1,-3,-2, 5,-1,-3,-1, 0,-1,-3,-2,-2, 0, 1,-1,-4},
+    {-1,-1,-2,-3,-1, 0,-2,-3,-2, 1, 2,-1, 5, 0,-2,-1,-1,-1,-1, 1,-3,-1,-1,-4},
+    {-2,-3,-3,-3,-2,-3,-3,-3,-1, 0, 0,-3, 0, 6,-4,-2,-2, 1, 3,-1,-3,-3,-1,-4},
+    {-1,-2,-2,-1,-3,-1,-1,-2,-2,-3,-3,-1,-2,-4, 7,-1,-1,-4,-3,-2,-2,-1,-2,-4},
+    { 1,-1, 1, 0,-1, 0, 0, 0,-1,-2,-2, 0,-1,-2,-1, 4, 1,-3,-2,-2, 0, 0, 0,-4},
+    { 0,-1, 0,-1,-1,-1,-1,-2,-2,-1,-1,-1,-1,-2,-1, 1, 5,-2,-2, 0,-1,-1, 0,-4},
+    {-3,-3,-4,-4,-2,-2,-3,-2,-2,-3,-2,-3,-1, 1,-4,-3,-2,11, 2,-3,-4,-3,-2,-4},
+    {-2,-2,-2,-3,-2,-1,-2,-3, 2,-1,-1,-2,-1, 3,-3,-2,-2, 2, 7,-1,-3,-2,-1,-4},
+    { 0,-3,-3,-3,-1,-2,-2,-3,-3, 3, 1,-2, 1,-1,-2,-2, 0,-3,-1, 4,-3,-2,-1,-4},
+    {-2,-1, 3, 4,-3, 0, 1,-1, 0,-3,-4, 0,-3,-3,-2, 0,-1,-4,-3,-3, 4, 1,-1,-4},
+    {-1, 0, 0, 1,-3, 3, 4,-2, 0,-3,-3, 1,-1,-3,-1, 0,-1,-3,-2,-2, 1, 4,-1,-4},
+    { 0,-1,-1,-1,-2,-1,-1,-1,-1,-1,-1,-1,-1,-1,-2, 0, 0,-2,-1,-1,-1,-1,-1,-4},
+    {-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4, 1},
+};
+
+void blosum62(int8_t *out)
+{
+    for (int a = 0; a < PG_NRES; ++a)
+        for (int b = 0; b < PG_NRES; ++b) {
+            const int aa = a == 24 ? 10 : a, bb = b == 24 ? 10 : b;
+            out[a * PG_NRES + b] = (int8_t)kB62[aa][bb];
+        }
+}
+
+struct Encoder {
+    uint8_t t[256];
+    Encoder()
+    {
+        const char *letters = "ARNDCQEGHILKMFPSTWYVBZX*J";
+        for (int i = 0; i < 256; ++i) t[i] = 22;  // X
+        for (int i = 0; i < PG_NRES; ++i) {
+            t[(unsigned char)letters[i]] = (uint8_t)i;
+            if (letters[i] >= 'A' && letters[i] <= 'Z')
+                t[(unsigned char)(letters[i] - 'A' + 'a')] = (uint8_t)i;
+        }
+    }
+};
+const Encoder kEnc;
+
+struct Side {
+    uint8_t *seq = nullptr;
+    uint64_t *offs = nullptr;
+    uint64_t n = 0;
+    uint32_t maxlen = 0;
+};
+
+size_t next_pow2(size_t x)
+{
+    size_t p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+}  // namespace
+
+struct pg_ctx {
+    pg_config cfg{};
+    int go = 0, ge = 0, xg = 0;
+    int8_t sm[PG_NRES * PG_NRES];
+    int8_t *d_sm = nullptr;
+    cudaStream_t stream = nullptr;
+    int nsm = 0;
+    int grid = 0;                  // persistent blocks
+    Side side[2];
+    bool cols_share_rows = false;
+    // scratch
+    unsigned int *d_counter = nullptr;
+    int *d_status = nullptr;
+    unsigned long long *d_exec = nullptr;
+    pg::Edge *d_bnd = nullptr;
+    uint64_t bnd_stride = 0;
+    size_t bnd_warps = 0;
+    int *d_gring = nullptr;
+    int gring_w = 0;
+    size_t gring_warps = 0;
+    // staging for the host-buffer entry point
+    pg_pair *d_pairs = nullptr;
+    pg_result *d_out = nullptr;
+    uint64_t cap = 0;
+    int last_launches = 0;
+    unsigned long long exec_total = 0;
+};
+
+extern "C" {
+
+void pg_config_default(pg_config *cfg, int32_t mode)
+{
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof *cfg);
+    cfg->mode = mode;
+    cfg->gap_open = -11;
+    cfg->gap_ext = -2;
+    cfg->gap_semantics = PG_GAPS_AS_CALLED;
+    cfg->xdrop = 49;
+    cfg->seed_len = 6;
+    cfg->seed_count = 2;
+    cfg->tie = 0;
+    cfg->flags = 0;
+    cfg->ani_thr = 30;
+    cfg->cov_thr = 0.7;
+    cfg->device = 0;
+    cfg->score_matrix = nullptr;
+}
+
+const char *pg_strerror(int code)
+{
+    switch (code) {
+    case PG_OK: return "ok";
+    case PG_ERR_ARG: return "invalid argument";
+    case PG_ERR_CUDA: return "CUDA error";
+    case PG_ERR_OOM: return "out of memory";
+    case PG_ERR_TIMEOUT: return "device wait timed out";
+    case PG_ERR_STATE: return "invalid call order";
+    case PG_ERR_RANGE: return "sequence longer than 65535 residues";
+    case PG_ERR_NODEV: return "no usable CUDA device";
+    default: return "unknown error";
+    }
+}
+
+const char *pg_last_error(void) { return g_err; }
+
+const char *pg_version(void) { return "pastis_gb300 0.1 (sm_103a)"; }
+
+void pg_destroy(pg_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->cfg.device);
+    for (int s = 0; s < 2; ++s) {
+        if (s == 1 && ctx->cols_share_rows) break;
+        cudaFree(ctx->side[s].seq);
+        cudaFree(ctx->side[s].offs);
+    }
+    cudaFree(ctx->d_sm);
+    cudaFree(ctx->d_counter);
+    cudaFree(ctx->d_status);
+    cudaFree(ctx->d_exec);
+    cudaFree(ctx->d_bnd);
+    cudaFree(ctx->d_gring);
+    cudaFree(ctx->d_pairs);
+    cudaFree(ctx->d_out);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+static int validate(const pg_config *c)
+{
+    if (c->mode != PG_MODE_SW && c->mode != PG_MODE_XDROP) return fail(PG_ERR_ARG, "mode %d", c->mode);
+    if (c->gap_semantics != PG_GAPS_AS_CALLED && c->gap_semantics != PG_GAPS_NOMINAL)
+        return fail(PG_ERR_ARG, "gap_semantics %d", c->gap_semantics);
+    if (c->gap_open < -1000 || c->gap_open > 1000 || c->gap_ext < -1000 || c->gap_ext > 1000)
+        return fail(PG_ERR_ARG, "gap scores must lie in [-1000, 1000]");
+    if (c->xdrop < 0 || c->xdrop > (1 << 28)) return fail(PG_ERR_ARG, "xdrop %d", c->xdrop);
+    if (c->seed_len < 1 || c->seed_len > 65535) return fail(PG_ERR_ARG, "seed_len %d", c->seed_len);
+    if (c->seed_count < 0) return fail(PG_ERR_ARG, "seed_count %d", c->seed_count);
+    if (c->tie < 0 || c->tie > 3) return fail(PG_ERR_ARG, "tie %d", c->tie);
+    if (c->flags & ~PG_F_SKIP_SPURIOUS_SEED) return fail(PG_ERR_ARG, "flags %d", c->flags);
+    return PG_OK;
+}
+
+int pg_create(const pg_config *cfg, pg_ctx **out)
+{
+    if (!cfg || !out) return fail(PG_ERR_ARG, "null argument");
+    *out = nullptr;
+    int rc = validate(cfg);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(PG_ERR_NODEV, "no CUDA device");
+    if (cfg->device < 0 || cfg->device >= ndev) return fail(PG_ERR_NODEV, "device %d of %d", cfg->device, ndev);
+    CU(cudaSetDevice(cfg->device));
+    pg_ctx *c = new (std::nothrow) pg_ctx();
+    if (!c) return fail(PG_ERR_OOM, "host allocation");
+    c->cfg = *cfg;
+    c->cfg.score_matrix = nullptr;
+    if (cfg->score_matrix) std::memcpy(c->sm, cfg->score_matrix, sizeof c->sm);
+    else blosum62(c->sm);
+    if (cfg->gap_semantics == PG_GAPS_AS_CALLED) {
+        // seqan Score(gapExtend, gapOpen) receives (gap_open, gap_ext)
+        c->go = cfg->gap_ext; c->ge = cfg->gap_open; c->xg = cfg->gap_open;
+    } else {
+        c->go = cfg->gap_open; c->ge = cfg->gap_ext; c->xg = cfg->gap_ext;
+    }
+#define CUD(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { pg_destroy(c); \
+        return fail(e_ == cudaErrorMemoryAllocation ? PG_ERR_OOM : PG_ERR_CUDA, "%s: %s", #call, \
+                    cudaGetErrorString(e_)); } } while (0)
+    CUD(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CUD(cudaMalloc(&c->d_sm, sizeof c->sm));
+    CUD(cudaMemcpy(c->d_sm, c->sm, sizeof c->sm, cudaMemcpyHostToDevice));
+    CUD(cudaMalloc(&c->d_counter, sizeof(unsigned int)));
+    CUD(cudaMalloc(&c->d_status, sizeof(int)));
+    CUD(cudaMalloc(&c->d_exec, sizeof(unsigned long long)));
+    CUD(cudaMemset(c->d_exec, 0, sizeof(unsigned long long)));
+    CUD(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, cfg->device));
+    int per_sm = 0;
+    if (cfg->mode == PG_MODE_XDROP)
+        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pg::k_xdrop<0>, pg::WARPS * 32, 0));
+    else
+        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pg::k_sw<0>, pg::WARPS * 32, 0));
+    if (per_sm < 1) per_sm = 1;
+    c->grid = c->nsm * per_sm;
+#undef CUD
+    *out = c;
+    return PG_OK;
+}
+
+// per-warp scratch for the current sequence set
+static int ensure_scratch(pg_ctx *c)
+{
+    const uint32_t rmax = c->side[0].maxlen;
+    const uint32_t cmax = c->cols_share_rows ? rmax : c->side[1].maxlen;
+    const uint64_t stride = (uint64_t)cmax + 1;
+    // keep the row scratch within 8 GiB: fewer resident warps for very long sequences
+    const size_t want_warps = (size_t)c->grid * pg::WARPS;
+    size_t warps = want_warps;
+    const size_t per_warp = stride * sizeof(pg::Edge);
+    const size_t budget = (size_t)8 << 30;
+    if (per_warp * warps > budget) {
+        warps = std::max<size_t>(pg::WARPS, budget / per_warp / pg::WARPS * pg::WARPS);
+        c->grid = (int)(warps / pg::WARPS);
+    }
+    if (stride > c->bnd_stride || warps > c->bnd_warps || !c->d_bnd) {
+        cudaFree(c->d_bnd);
+        c->d_bnd = nullptr;
+        CU(cudaMalloc(&c->d_bnd, per_warp * warps));
+        c->bnd_stride = stride;
+        c->bnd_warps = warps;
+    }
+    const int gw = (int)next_pow2((size_t)std::max(rmax, cmax) + 4);
+    if (gw > c->gring_w || warps > c->gring_warps || !c->d_gring) {
+        cudaFree(c->d_gring);
+        c->d_gring = nullptr;
+        CU(cudaMalloc(&c->d_gring, (size_t)3 * gw * sizeof(int) * warps));
+        c->gring_w = gw;
+        c->gring_warps = warps;
+    }
+    return PG_OK;
+}
+
+int pg_set_seqs(pg_ctx *c, int32_t side, const char *residues, const uint64_t *offsets, uint64_t n)
+{
+    if (!c || (side != 0 && side != 1) || !offsets || (n > 0 && !residues))
+        return fail(PG_ERR_ARG, "pg_set_seqs: bad argument");
+    CU(cudaSetDevice(c->cfg.device));
+    const uint64_t total = offsets[n] - offsets[0];
+    uint32_t maxlen = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        if (offsets[i + 1] < offsets[i]) return fail(PG_ERR_ARG, "offsets not ascending at %llu", (unsigned long long)i);
+        const uint64_t len = offsets[i + 1] - offsets[i];
+        if (len > 65535) return fail(PG_ERR_RANGE, "sequence %llu has %llu residues", (unsigned long long)i, (unsigned long long)len);
+        maxlen = std::max<uint32_t>(maxlen, (uint32_t)len);
+    }
+    uint8_t *codes = (uint8_t *)std::malloc(total ? total : 1);
+    uint64_t *offs = (uint64_t *)std::malloc((n + 1) * sizeof(uint64_t));
+    if (!codes || !offs) { std::free(codes); std::free(offs); return fail(PG_ERR_OOM, "host staging"); }
+    const uint8_t *src = (const uint8_t *)residues + offsets[0];
+    for (uint64_t q = 0; q < total; ++q) codes[q] = kEnc.t[src[q]];
+    for (uint64_t i = 0; i <= n; ++i) offs[i] = offsets[i] - offsets[0];
+    Side &s = c->side[side];
+    if (side == 1 && c->cols_share_rows) { s = Side(); c->cols_share_rows = false; }
+    if (side == 0 && c->cols_share_rows) { c->side[1] = Side(); c->cols_share_rows = false; }
+    cudaFree(s.seq); cudaFree(s.offs);
+    s = Side();
+    cudaError_t e1 = cudaMalloc(&s.seq, total ? total : 1);
+    cudaError_t e2 = e1 == cudaSuccess ? cudaMalloc(&s.offs, (n + 1) * sizeof(uint64_t)) : e1;
+    cudaError_t e3 = e2 == cudaSuccess ? cudaMemcpy(s.seq, codes, total, cudaMemcpyHostToDevice) : e2;
+    cudaError_t e4 = e3 == cudaSuccess ? cudaMemcpy(s.offs, offs, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice) : e3;
+    std::free(codes);
+    std::free(offs);
+    if (e4 != cudaSuccess) {
+        cudaFree(s.seq); cudaFree(s.offs); s = Side();
+        return fail(e4 == cudaErrorMemoryAllocation ? PG_ERR_OOM : PG_ERR_CUDA, "pg_set_seqs: %s", cudaGetErrorString(e4));
+    }
+    s.n = n;
+    s.maxlen = maxlen;
+    return ensure_scratch(c);
+}
+
+int pg_share_row_seqs(pg_ctx *c)
+{
+    if (!c) return fail(PG_ERR_ARG, "null context");
+    if (!c->side[0].seq) return fail(PG_ERR_STATE, "row sequences not set");
+    CU(cudaSetDevice(c->cfg.device));
+    if (!c->cols_share_rows) { cudaFree(c->side[1].seq); cudaFree(c->side[1].offs); }
+    c->side[1] = c->side[0];
+    c->cols_share_rows = true;
+    return ensure_scratch(c);
+}
+
+static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, uint64_t coff,
+                  pg_result *d_out, cudaStream_t st)
+{
+    c->last_launches = 0;
+    if (n == 0) return PG_OK;
+    if (!c->side[0].seq || !c->side[1].seq) return fail(PG_ERR_STATE, "sequences not set");
+    if (n > 0xffffffffull) return fail(PG_ERR_ARG, "batch of %llu pairs exceeds 2^32-1", (unsigned long long)n);
+    pg::KParams kp;
+    kp.pairs = d_pairs; kp.n = n; kp.roff = roff; kp.coff = coff;
+    kp.rseq = c->side[0].seq; kp.roffs = c->side[0].offs; kp.nr = c->side[0].n;
+    kp.cseq = c->side[1].seq; kp.coffs = c->side[1].offs; kp.nc = c->side[1].n;
+    kp.out = d_out; kp.sm = c->d_sm;
+    kp.go = c->go; kp.ge = c->ge; kp.xg = c->xg; kp.xdrop = c->cfg.xdrop;
+    kp.seed_len = c->cfg.seed_len; kp.seed_count = c->cfg.seed_count; kp.flags = c->cfg.flags;
+    kp.ani_thr = c->cfg.ani_thr; kp.cov_thr = c->cfg.cov_thr;
+    kp.counter = c->d_counter; kp.status = c->d_status; kp.exec_cells = c->d_exec;
+    kp.bnd = c->d_bnd; kp.bnd_stride = c->bnd_stride;
+    kp.gring = c->d_gring; kp.gring_w = c->gring_w;
+    CU(cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned int), st));
+    CU(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
+    const uint64_t need_blocks = (n + pg::WARPS - 1) / pg::WARPS;
+    const int grid = (int)std::min<uint64_t>((uint64_t)c->grid, need_blocks);
+    const dim3 blk(pg::WARPS * 32);
+    if (c->cfg.mode == PG_MODE_XDROP) {
+        switch (c->cfg.tie) {
+        case 0: pg::k_xdrop<0><<<grid, blk, 0, st>>>(kp); break;
+        case 1: pg::k_xdrop<1><<<grid, blk, 0, st>>>(kp); break;
+        case 2: pg::k_xdrop<2><<<grid, blk, 0, st>>>(kp); break;
+        default: pg::k_xdrop<3><<<grid, blk, 0, st>>>(kp); break;
+        }
+    } else {
+        switch (c->cfg.tie) {
+        case 0: pg::k_sw<0><<<grid, blk, 0, st>>>(kp); break;
+        case 1: pg::k_sw<1><<<grid, blk, 0, st>>>(kp); break;
+        case 2: pg::k_sw<2><<<grid, blk, 0, st>>>(kp); break;
+        default: pg::k_sw<3><<<grid, blk, 0, st>>>(kp); break;
+        }
+    }
+    CU(cudaGetLastError());
+    c->last_launches = 1;
+    return PG_OK;
+}
+
+static int check_status(pg_ctx *c)
+{
+    int st = 0;
+    CU(cudaMemcpy(&st, c->d_status, sizeof st, cudaMemcpyDeviceToHost));
+    if (st & pg::ST_BAD_INDEX) return fail(PG_ERR_ARG, "a pair refers to a sequence index out of range");
+    return PG_OK;
+}
+
+int pg_align_device(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, uint64_t coff,
+                    pg_result *d_out, void *stream)
+{
+    if (!c || (n > 0 && (!d_pairs || !d_out))) return fail(PG_ERR_ARG, "pg_align_device: bad argument");
+    CU(cudaSetDevice(c->cfg.device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    return launch(c, d_pairs, n, roff, coff, d_out, st);
+}
+
+int pg_sync(pg_ctx *c)
+{
+    if (!c) return fail(PG_ERR_ARG, "null context");
+    CU(cudaSetDevice(c->cfg.device));
+    CU(cudaDeviceSynchronize());
+    return check_status(c);
+}
+
+int pg_align(pg_ctx *c, const pg_pair *pairs, uint64_t n, uint64_t roff, uint64_t coff, pg_result *out)
+{
+    if (!c || (n > 0 && (!pairs || !out))) return fail(PG_ERR_ARG, "pg_align: bad argument");
+    c->last_launches = 0;
+    if (n == 0) return PG_OK;
+    CU(cudaSetDevice(c->cfg.device));
+    if (n > c->cap) {
+        cudaFree(c->d_pairs); cudaFree(c->d_out);
+        c->d_pairs = nullptr; c->d_out = nullptr; c->cap = 0;
+        CU(cudaMalloc(&c->d_pairs, n * sizeof(pg_pair)));
+        CU(cudaMalloc(&c->d_out, n * sizeof(pg_result)));
+        c->cap = n;
+    }
+    CU(cudaMemcpyAsync(c->d_pairs, pairs, n * sizeof(pg_pair), cudaMemcpyHostToDevice, c->stream));
+    int rc = launch(c, c->d_pairs, n, roff, coff, c->d_out, c->stream);
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(out, c->d_out, n * sizeof(pg_result), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return check_status(c);
+}
+
+int pg_last_launches(const pg_ctx *c) { return c ? c->last_launches : 0; }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- DPX peak
+// Throughput of the DPX add-max instruction (__viaddmax_s32, max(a + b, c)) over
+// every SM: 8 independent chains per thread, so the pipe, not latency, limits.
+namespace {
+template <int CHAINS>
+__global__ void k_dpx_peak(int iters, int b, int *sink)
+{
+    int a[CHAINS];
+#pragma unroll
+    for (int k = 0; k < CHAINS; ++k) a[k] = threadIdx.x + k;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < CHAINS; ++k) a[k] = __viaddmax_s32(a[k], b, a[(k + 1) % CHAINS]);
+    }
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < CHAINS; ++k) s ^= a[k];
+    if (s == 0x7fffffff) sink[blockIdx.x] = s;
+}
+}  // namespace
+
+extern "C" {
+
+int pg_dpx_peak(int device, double *ops_per_s)
+{
+    if (!ops_per_s) return fail(PG_ERR_ARG, "null output");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+        return fail(PG_ERR_NODEV, "device %d", device);
+    CU(cudaSetDevice(device));
+    int nsm = 0;
+    CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+    const int threads = 1024, blocks = nsm * 2, iters = 4096;
+    int *sink = nullptr;
+    CU(cudaMalloc(&sink, blocks * sizeof(int)));
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    k_dpx_peak<8><<<blocks, threads>>>(iters, -1, sink);  // warm-up
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; ++rep) {
+        cudaEventRecord(e0);
+        k_dpx_peak<8><<<blocks, threads>>>(iters, -1, sink);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) best = ms;
+    }
+    cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (err != cudaSuccess) return fail(PG_ERR_CUDA, "dpx peak: %s", cudaGetErrorString(err));
+    *ops_per_s = (double)threads * blocks * iters * 8 / (best * 1e-3);
+    return PG_OK;
+}
+
+// cells computed by the kernels since the context was created
+unsigned long long pg_exec_cells(pg_ctx *c)
+{
+    if (!c) return 0;
+    unsigned long long v = 0;
+    cudaSetDevice(c->cfg.device);
+    cudaMemcpy(&v, c->d_exec, sizeof v, cudaMemcpyDeviceToHost);
+    return v;
+}
+
+}  // extern "C"

@@ -1,0 +1,134 @@
+// pg_xdrop.cuh -- warp-level gapped X-drop extension (sm_103a).
+//
+// Restates seqan::extendSeed(seed, H, V, EXTEND_BOTH, score, x, GappedXDrop())
+// as PASTIS calls it (src/align/SeqanXdropAligner.cpp:281-283), one direction
+// at a time, by anti-diagonals of the (V consumed = column, H consumed = row)
+// grid with a linear gap g:
+//   T(c, r) = max(T(c-1, r) + g, T(c, r-1) + g, T(c-1, r-1) + s)
+// A cell below best - X is dead; best is the maximum over completed
+// anti-diagonals.  The band [lo, hi) of computed columns is trimmed of dead
+// cells at both ends (current and previous anti-diagonal), widened by one on
+// the right and clipped to the grid; the extension stops when it is empty.
+// End point: the far corner if alive, else a fixed probe of the previous
+// anti-diagonal, else the first maximum two anti-diagonals back.
+//
+// The three live anti-diagonals sit in a ring of W ints each (column c at slot
+// c & (W-1)); lanes own consecutive columns of the band.  A band wider than the
+// ring makes the routine report overflow so the caller can rerun the direction
+// with a larger ring.
+#pragma once
+#include <cstdint>
+
+#include "pg_dp.cuh"
+
+namespace pg {
+
+constexpr int UND = NEG;  // dead cell
+
+struct XdOut {
+    int dv, dh;        // residues consumed in V and in H
+    uint32_t cells;    // band cells computed
+    int ok;            // 0: ring overflow
+};
+
+// V / Hs point at the first residue to consume; vstep / hstep are +1 or -1.
+__device__ XdOut xdrop_dir_warp(const uint8_t *__restrict__ V, int nv, int vstep,
+                                const uint8_t *__restrict__ Hs, int nh, int hstep,
+                                const int *__restrict__ ssm, int g, int X,
+                                int *ring, int W)
+{
+    const int lane = threadIdx.x & 31;
+    XdOut o{0, 0, 0u, 1};
+    const int cols = nv + 1, rows = nh + 1;
+    if (cols == 1 || rows == 1) return o;
+    const int mask = W - 1;
+    int *A1 = ring, *A2 = ring + W, *A3 = ring + 2 * W;
+    int off1 = 0, len1 = 0, off2 = 0, len2 = 1, off3 = 0, len3 = 2;
+    if (lane == 0) {
+        A2[0] = 0;
+        const int v1 = (-g > X) ? UND : g;
+        A3[0] = v1;
+        A3[1] = v1;
+    }
+    __syncwarp();
+    int best = 0, d = 1, lo = 1, hi = 2;
+    while (lo < hi) {
+        ++d;
+        int *t = A1; A1 = A2; A2 = A3; A3 = t;
+        off1 = off2; len1 = len2;
+        off2 = off3; len2 = len3;
+        off3 = lo - 1; len3 = hi + 1 - off3;
+        if (len3 > W) { o.ok = 0; return o; }
+        const int thr = best - X;
+        int lbest = d * g;
+        for (int c = lo + lane; c < hi; c += 32) {
+            const int r = d - c;
+            int v = max(A2[(c - 1) & mask], A2[c & mask]) + g;
+            const int vr = __ldg(V + vstep * (c - 1));
+            const int hr = __ldg(Hs + hstep * (r - 1));
+            const int dg = A1[(c - 1) & mask] + ssm[vr * 32 + hr];
+            v = max(v, dg);
+            const bool live = v >= thr;
+            A3[c & mask] = live ? v : UND;
+            if (live) lbest = max(lbest, v);
+        }
+        if (lane == 0) {
+            const int bval = (d * g > best - X) ? d * g : UND;
+            A3[off3 & mask] = (off3 == 0) ? bval : UND;
+            A3[hi & mask] = (d == hi && hi < cols) ? bval : UND;
+        }
+        __syncwarp();
+        const int db = __reduce_max_sync(FULL, lbest);
+        if (db > best) best = db;
+        o.cells += (uint32_t)(hi - lo);
+        // advance lo past columns whose cell and left predecessor are dead
+        for (int c0 = lo;; c0 += 32) {
+            const int c = c0 + lane;
+            bool cond = (c - off3 < len3);
+            if (cond) cond = A3[c & mask] == UND;
+            if (cond) cond = (c - off2 - 1 < len2);
+            if (cond) cond = A2[(c - 1) & mask] == UND;
+            const unsigned bal = __ballot_sync(FULL, !cond);
+            if (bal) { lo = c0 + __ffs(bal) - 1; break; }
+        }
+        // pull hi back over dead columns
+        for (int c0 = hi;; c0 -= 32) {
+            const int c = c0 - lane;
+            bool cond = (c - off3 > 0);
+            if (cond) cond = A3[(c - 1) & mask] == UND;
+            if (cond) cond = A2[(c - 1) & mask] == UND;
+            const unsigned bal = __ballot_sync(FULL, !cond);
+            if (bal) { hi = c0 - (__ffs(bal) - 1); break; }
+        }
+        ++hi;
+        if (lo < d + 2 - rows) lo = d + 2 - rows;
+        if (hi > cols) hi = cols;
+        __syncwarp();
+    }
+
+    int lc = off3 + len3 - 2, lr = d - lc, ls = A3[lc & mask];
+    if (ls == UND) {
+        const int ca = off2 + len2 - 2;
+        if (A2[ca & mask] != UND) {
+            lc = ca; lr = d - 1 - lc; ls = A2[ca & mask];
+        } else if (len2 > 2 && A2[(ca - 1) & mask] != UND) {
+            lc = ca - 1; lr = d - 1 - lc; ls = A2[(ca - 1) & mask];
+        }
+    }
+    if (ls == UND) {
+        int bv = UND, bc = 0x7fffffff;
+        for (int k = lane; k < len1; k += 32) {
+            const int val = A1[(off1 + k) & mask];
+            if (val > bv) { bv = val; bc = off1 + k; }
+        }
+        const int mv = __reduce_max_sync(FULL, bv);
+        const unsigned cand = (bv == mv) ? (unsigned)bc : 0x7fffffffu;
+        const int mc = (int)__reduce_min_sync(FULL, cand);
+        if (mv != UND) { ls = mv; lc = mc; lr = d - 2 - lc; }
+    }
+    if (ls != UND) { o.dv = lc; o.dh = lr; }
+    __syncwarp();
+    return o;
+}
+
+}  // namespace pg

@@ -1,0 +1,111 @@
+"""Seeded synthetic workloads (the stand-in for the reference's FASTA input and
+its k-mer SpGEMM candidate pairs), generated by libpastis_synth.so.
+
+Workload presets follow the benchmark definitions of this stage:
+
+  sw100k     100k pairs from 20k proteins, lognormal lengths (median 250,
+             sigma 0.5, clamp 30-1000), half homologs at 30-80 % identity with
+             2 % indels (geometric, mean 3), local SW
+  xdrop1m    1M pairs of the same generator, up to 2 seeds = shared exact
+             6-mers, X-drop x = 49
+  uneven10m  10M pairs, lengths 80 % lognormal (median 300) + 20 % uniform
+             1000-5000, min 20
+"""
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi
+
+
+class SynthCfg(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_uint64), ("nseqs", ctypes.c_uint64),
+                ("fam_min", ctypes.c_uint32), ("fam_max", ctypes.c_uint32),
+                ("len_median", ctypes.c_double), ("len_sigma", ctypes.c_double),
+                ("len_min", ctypes.c_uint32), ("len_max", ctypes.c_uint32),
+                ("mix_frac", ctypes.c_double), ("mix_lo", ctypes.c_uint32),
+                ("mix_hi", ctypes.c_uint32), ("id_lo", ctypes.c_double),
+                ("id_hi", ctypes.c_double), ("indel_rate", ctypes.c_double),
+                ("indel_mean", ctypes.c_double), ("npairs", ctypes.c_uint64),
+                ("homolog_frac", ctypes.c_double), ("k", ctypes.c_uint32),
+                ("alph", ctypes.c_int32)]
+
+
+@dataclass
+class Workload:
+    name: str
+    seq: np.ndarray          # residue codes (0..19), concatenated
+    offs: np.ndarray         # uint64, nseqs + 1
+    pairs: np.ndarray        # capi.PAIR_DTYPE
+    homolog: np.ndarray      # uint8 per pair
+    spurious: np.ndarray     # uint8 per pair: no shared k-mer, random seed
+    family: np.ndarray
+    params: dict = field(default_factory=dict)
+
+    @property
+    def ascii(self):
+        return capi.decode(self.seq)
+
+    def lengths(self):
+        return np.diff(self.offs).astype(np.int64)
+
+    def sw_cells(self):
+        L = self.lengths()
+        return int((L[self.pairs["row"]] * L[self.pairs["col"]]).sum())
+
+    def subset(self, idx):
+        return Workload(self.name, self.seq, self.offs, self.pairs[idx], self.homolog[idx],
+                        self.spurious[idx], self.family, dict(self.params))
+
+
+PRESETS = {
+    "sw100k": dict(nseqs=20_000, npairs=100_000, len_median=250.0, len_sigma=0.5, len_min=30,
+                   len_max=1000, mix_frac=0.0, mix_lo=0, mix_hi=0, id_lo=0.30, id_hi=0.80,
+                   homolog_frac=0.5, k=6, alph=0, fam_min=6, fam_max=6),
+    "xdrop1m": dict(nseqs=200_000, npairs=1_000_000, len_median=250.0, len_sigma=0.5, len_min=30,
+                    len_max=1000, mix_frac=0.0, mix_lo=0, mix_hi=0, id_lo=0.30, id_hi=0.80,
+                    homolog_frac=0.5, k=6, alph=0, fam_min=6, fam_max=6),
+    "uneven10m": dict(nseqs=2_000_000, npairs=10_000_000, len_median=300.0, len_sigma=0.5,
+                      len_min=20, len_max=5000, mix_frac=0.2, mix_lo=1000, mix_hi=5000,
+                      id_lo=0.30, id_hi=0.80, homolog_frac=0.5, k=6, alph=0, fam_min=6,
+                      fam_max=6),
+}
+
+
+def generate(preset="xdrop1m", seed=20260101, scale=1.0, **over):
+    """Generate a workload; scale multiplies the sequence and pair counts."""
+    p = dict(PRESETS[preset])
+    p.update(over)
+    c = SynthCfg()
+    c.seed = seed
+    c.nseqs = max(2, int(round(p["nseqs"] * scale)))
+    c.npairs = max(1, int(round(p["npairs"] * scale)))
+    for k in ("fam_min", "fam_max", "len_median", "len_sigma", "len_min", "len_max", "mix_frac",
+              "mix_lo", "mix_hi", "id_lo", "id_hi", "homolog_frac", "k", "alph"):
+        setattr(c, k, p[k])
+    c.indel_rate = p.get("indel_rate", 0.02)
+    c.indel_mean = p.get("indel_mean", 3.0)
+    lib = capi.load("libpastis_synth.so")
+    h = lib.pg_synth_generate(ctypes.byref(c))
+    if not h:
+        raise MemoryError("synthetic generator failed")
+    try:
+        ns, nres, npairs = lib.pg_synth_nseqs(h), lib.pg_synth_nres(h), lib.pg_synth_npairs(h)
+
+        def arr(ptr, dtype, n):
+            if n == 0:
+                return np.zeros(0, dtype=dtype)
+            buf = (ctypes.c_char * (n * np.dtype(dtype).itemsize)).from_address(ptr)
+            return np.frombuffer(buf, dtype=dtype).copy()
+
+        w = Workload(preset, arr(lib.pg_synth_seq(h), np.uint8, nres),
+                     arr(lib.pg_synth_offs(h), np.uint64, ns + 1),
+                     arr(lib.pg_synth_pairs(h), capi.PAIR_DTYPE, npairs),
+                     arr(lib.pg_synth_homolog(h), np.uint8, npairs),
+                     arr(lib.pg_synth_spurious(h), np.uint8, npairs),
+                     arr(lib.pg_synth_family(h), np.uint32, ns),
+                     dict(p, seed=seed, scale=scale))
+    finally:
+        lib.pg_synth_free(h)
+    return w

@@ -1,0 +1,234 @@
+"""GPU kernels (through the C ABI) against the CPU oracle, every output field
+bit for bit: score, coordinates, columns, matches, gap runs, identity,
+score_aln, flags, seed choice and the per-pair cell count."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["score", "aln_len", "matches", "gap_opens", "beg_h", "end_h", "beg_v", "end_v",
+          "identity", "score_aln", "seed_used", "flags", "cells"]
+
+
+def oracle_params(O, cfg):
+    from pastis_gb300 import capi
+    first, ext, xg = capi.resolved_gaps(cfg)
+    return O.make_params(gap_first=first, gap_ext=ext, xdrop_gap=xg, xdrop=cfg.xdrop,
+                         seed_len=cfg.seed_len, seed_count=cfg.seed_count, tie=cfg.tie,
+                         flags=cfg.flags, cov_thr=cfg.cov_thr, ani_thr=cfg.ani_thr)
+
+
+def assert_same(got, exp, pairs=None):
+    bad = np.zeros(len(got), dtype=bool)
+    for f in FIELDS:
+        a, b = got[f], exp[f]
+        if f in ("identity", "score_aln"):
+            a, b = a.view(np.uint32), b.view(np.uint32)
+        bad |= a != b
+    if bad.any():
+        i = int(np.flatnonzero(bad)[0])
+        diff = {f: (got[f][i], exp[f][i]) for f in FIELDS if got[f][i] != exp[f][i]}
+        raise AssertionError("%d of %d pairs differ; first #%d %s pair=%s" % (
+            bad.sum(), len(got), i, diff, None if pairs is None else pairs[i]))
+
+
+def run_both(mode, w, cfg, O, pairs=None, roff=0, coff=0, share=True):
+    from pastis_gb300 import capi
+    pairs = w.pairs if pairs is None else pairs
+    ctx = capi.Context(cfg)
+    ascii_ = w.ascii
+    ctx.set_seqs(0, ascii_, w.offs)
+    if share:
+        ctx.share_row_seqs()
+    else:
+        ctx.set_seqs(1, ascii_, w.offs)
+    got = ctx.align(pairs, roff, coff)
+    assert ctx.last_launches() == 1
+    codes = O.encode(bytes(ascii_))
+    exp = O.batch(mode, codes, w.offs, codes, w.offs, pairs, oracle_params(O, cfg),
+                  bl_roff=roff, bl_coff=coff)
+    ctx.close()
+    return got, exp
+
+
+@pytest.fixture(scope="module")
+def sw_small(native):
+    from pastis_gb300 import synth
+    return synth.generate("sw100k", seed=101, scale=0.02)
+
+
+@pytest.fixture(scope="module")
+def xd_small(native):
+    from pastis_gb300 import synth
+    return synth.generate("xdrop1m", seed=202, scale=0.005)
+
+
+@pytest.mark.parametrize("tie", [0, 1, 2, 3])
+@pytest.mark.parametrize("gaps", [0, 1])
+def test_sw_parity(sw_small, oracle_mod, tie, gaps):
+    from pastis_gb300 import capi
+    cfg = capi.config(capi.MODE_SW, tie=tie, gap_semantics=gaps)
+    got, exp = run_both(0, sw_small, cfg, oracle_mod)
+    assert_same(got, exp, sw_small.pairs)
+    assert (got["flags"] & capi.RF_PASSED).any()
+
+
+@pytest.mark.parametrize("tie", [0, 1, 2, 3])
+@pytest.mark.parametrize("gaps", [0, 1])
+def test_xdrop_parity(xd_small, oracle_mod, tie, gaps):
+    from pastis_gb300 import capi
+    cfg = capi.config(capi.MODE_XDROP, tie=tie, gap_semantics=gaps)
+    got, exp = run_both(1, xd_small, cfg, oracle_mod)
+    assert_same(got, exp, xd_small.pairs)
+    assert (got["seed_used"] == 1).any() and (got["flags"] & capi.RF_PASSED).any()
+
+
+@pytest.mark.parametrize("flags,xdrop,seed_count", [(1, 49, 2), (0, 10, 2), (0, 200, 2),
+                                                      (0, 49, 1), (0, 0, 2)])
+def test_xdrop_switches(xd_small, oracle_mod, flags, xdrop, seed_count):
+    from pastis_gb300 import capi
+    cfg = capi.config(capi.MODE_XDROP, flags=flags, xdrop=xdrop, seed_count=seed_count)
+    got, exp = run_both(1, xd_small, cfg, oracle_mod)
+    assert_same(got, exp, xd_small.pairs)
+
+
+def test_long_sequences_row_blocks(native, oracle_mod):
+    """Lengths up to 5000: many row blocks through the per-warp scratch row."""
+    from pastis_gb300 import capi, synth
+    w = synth.generate("uneven10m", seed=303, scale=0.00003)
+    for mode in (capi.MODE_SW, capi.MODE_XDROP):
+        cfg = capi.config(mode)
+        got, exp = run_both(mode, w, cfg, oracle_mod)
+        assert_same(got, exp, w.pairs)
+    assert w.lengths().max() > 1000
+
+
+def test_wide_band_uses_global_ring(native, oracle_mod):
+    """Cheap gaps and a huge X make the X-drop band wider than the shared ring."""
+    from pastis_gb300 import capi, synth
+    w = synth.generate("xdrop1m", seed=404, scale=0.0003, len_median=900.0, len_max=3000)
+    cfg = capi.config(capi.MODE_XDROP, gap_semantics=capi.GAPS_NOMINAL, xdrop=5000)
+    got, exp = run_both(1, w, cfg, oracle_mod)
+    assert_same(got, exp, w.pairs)
+
+
+def _toy(seqs):
+    from pastis_gb300 import synth
+    from oracle import oracle as O
+    codes = [O.encode(s) for s in seqs]
+    offs = np.concatenate([[0], np.cumsum([len(c) for c in codes])]).astype(np.uint64)
+    seq = np.concatenate(codes) if codes else np.zeros(0, np.uint8)
+    return synth.Workload("toy", seq, offs, np.zeros(0, dtype=O.PAIR_DTYPE), np.zeros(0, np.uint8),
+                          np.zeros(0, np.uint8), np.zeros(len(seqs), np.uint32))
+
+
+EDGE_SEQS = ["", "W", "A", "ACDEFGHIKLMNPQRSTVWY", "acdefghiklmnpqrstvwy", "BZX*JBZX*J",
+             "UUOO??ACDE", "W" * 300, "MKVLAAGIVGLLLAC" * 20, "PPPPPPPPPP"]
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_edge_cases(native, oracle_mod, mode):
+    """Empty and length-1 sequences, non-standard and lower-case letters, seeds
+    at (0,0), seeds past the sequence end, identical pairs."""
+    from pastis_gb300 import capi
+    O = oracle_mod
+    w = _toy(EDGE_SEQS)
+    n = len(EDGE_SEQS)
+    L = np.diff(w.offs).astype(int)
+    rows, cols = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    pairs = np.zeros(n * n * 3, dtype=O.PAIR_DTYPE)
+    pairs["row"] = np.tile(rows.ravel(), 3)
+    pairs["col"] = np.tile(cols.ravel(), 3)
+    k = n * n
+    pairs["count"] = 1
+    # block 1: seeds at (0, 0); block 2: second seed mid-way; block 3: seeds past the end
+    pairs["rs1"][k:2 * k] = L[pairs["row"][k:2 * k]] // 2
+    pairs["cs1"][k:2 * k] = L[pairs["col"][k:2 * k]] // 2
+    pairs["count"][k:2 * k] = 2
+    pairs["rs0"][2 * k:] = L[pairs["row"][2 * k:]] + 3
+    pairs["cs0"][2 * k:] = np.maximum(L[pairs["col"][2 * k:]] - 2, 0)
+    cfg = capi.config(mode)
+    got, exp = run_both(mode, w, cfg, O, pairs=pairs)
+    assert_same(got, exp, pairs)
+    if mode == 1:
+        assert (got["flags"] & capi.RF_BAD_SEED).any()
+
+
+def test_block_offsets_and_separate_columns(sw_small, oracle_mod):
+    from pastis_gb300 import capi
+    pairs = sw_small.pairs[:500].copy()
+    pairs["row"] = pairs["row"] % 1000
+    pairs["col"] = pairs["col"] % 1000
+    cfg = capi.config(capi.MODE_SW)
+    got, exp = run_both(0, sw_small, cfg, oracle_mod, pairs=pairs, roff=37, coff=1234,
+                        share=False)
+    assert_same(got, exp, pairs)
+
+
+def test_errors_and_empty_batch(sw_small, native):
+    from pastis_gb300 import capi
+    ctx = capi.Context(capi.config(capi.MODE_SW))
+    with pytest.raises(capi.PgError) as e:
+        ctx.align(sw_small.pairs[:4])
+    assert e.value.code == capi.PG_ERR_STATE
+    ctx.set_seqs(0, sw_small.ascii, sw_small.offs)
+    ctx.share_row_seqs()
+    out = ctx.align(sw_small.pairs[:0])
+    assert len(out) == 0 and ctx.last_launches() == 0
+    bad = sw_small.pairs[:8].copy()
+    bad["row"][3] = len(sw_small.offs) + 5
+    with pytest.raises(capi.PgError) as e:
+        ctx.align(bad)
+    assert e.value.code == capi.PG_ERR_ARG
+    # the context stays usable after an error
+    ok = ctx.align(sw_small.pairs[:8])
+    assert (ok["cells"] > 0).all()
+    too_long = np.full(65536, ord("A"), dtype=np.uint8)
+    with pytest.raises(capi.PgError) as e:
+        ctx.set_seqs(0, too_long, np.array([0, 65536], dtype=np.uint64))
+    assert e.value.code == capi.PG_ERR_RANGE
+
+
+def test_max_length_sequence(native, oracle_mod):
+    """A 65535-residue sequence (the u16 limit of PASTIS, FastaData.hpp:109)."""
+    from pastis_gb300 import capi
+    O = oracle_mod
+    rng = np.random.default_rng(9)
+    letters = "ARNDCQEGHILKMFPSTWYV"
+    big = "".join(rng.choice(list(letters), 65535))
+    small = big[30000:30040]
+    w = _toy([big, small])
+    pairs = np.zeros(2, dtype=O.PAIR_DTYPE)
+    pairs["row"] = [0, 1]
+    pairs["col"] = [1, 0]
+    pairs["rs0"], pairs["cs0"] = [30010, 10], [10, 30010]
+    pairs["count"] = 1
+    for mode in (0, 1):
+        got, exp = run_both(mode, w, capi.config(mode), O, pairs=pairs)
+        assert_same(got, exp, pairs)
+
+
+def test_cpp_driver_on_gpu(sw_small, oracle_mod):
+    """The C++ pw_aln_batch with the GPU aligner equals the oracle-driven run."""
+    from pastis_gb300 import capi
+    O = oracle_mod
+    w = sw_small
+    pairs = w.pairs[:1500]
+    rows = pairs["row"].astype(np.uint64)
+    cols = pairs["col"].astype(np.uint64)
+    vals = np.zeros(len(pairs), dtype=capi.KMERLOC_DTYPE)
+    vals["count"] = pairs["count"]
+    vals["score"] = pairs["score"]
+    vals["first_r"], vals["first_c"] = pairs["rs0"], pairs["cs0"]
+    vals["second_r"], vals["second_c"] = pairs["rs1"], pairs["cs1"]
+    cfg = capi.config(capi.MODE_XDROP)
+    r_gpu, c_gpu, v_gpu, st = capi.pw_aln_batch(capi.MODE_XDROP, rows, cols, vals, w.ascii, w.offs,
+                                               batch_sz=400, ckthr=0, cfg=cfg)
+    codes = O.encode(bytes(w.ascii))
+    p = oracle_params(O, cfg)
+    r_cpu, c_cpu, v_cpu, st2 = capi.pw_aln_batch(
+        capi.MODE_XDROP, rows, cols, vals, w.ascii, w.offs, batch_sz=400, ckthr=0,
+        callback=lambda pr, ro, co: O.batch(1, codes, w.offs, codes, w.offs, pr, p, ro, co)["score_aln"])
+    assert st["nnz_aln"] == st2["nnz_aln"] and st["batches"] == 4
+    assert (r_gpu == r_cpu).all() and (c_gpu == c_cpu).all()
+    assert (v_gpu["score_aln"].view(np.uint32) == v_cpu["score_aln"].view(np.uint32)).all()

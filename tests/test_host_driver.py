@@ -1,0 +1,104 @@
+"""The C++ batch driver pw_aln_batch (mirror of src/DistPWRunner.cpp:25-165) on
+CPU, with the oracle plugged in as the aligner through the callback hook:
+k-mer threshold prune, --bsz batching (including the empty trailing batch),
+block offsets, and the post-prune of entries whose score_aln is 0."""
+import numpy as np
+import pytest
+
+
+def _block(seed=1, nseq=40, nnz=300):
+    rng = np.random.default_rng(seed)
+    from oracle import oracle as O
+    letters = np.frombuffer(O.LETTERS[:20].encode(), dtype=np.uint8)
+    seqs = []
+    for i in range(nseq):
+        if i % 2 and seqs:
+            s = seqs[-1].copy()
+            mut = rng.random(len(s)) < 0.25
+            s[mut] = letters[rng.integers(0, 20, mut.sum())]
+        else:
+            s = letters[rng.integers(0, 20, rng.integers(20, 90))]
+        seqs.append(s)
+    offs = np.concatenate([[0], np.cumsum([len(s) for s in seqs])]).astype(np.uint64)
+    res = np.concatenate(seqs)
+    rows = rng.integers(0, nseq - 4, nnz).astype(np.uint64)
+    cols = rows + rng.integers(0, 4, nnz).astype(np.uint64)
+    order = np.lexsort((rows, cols))
+    rows, cols = rows[order], cols[order]
+    return res, offs, rows, cols, rng
+
+
+def _oracle_cb(O, mode, res, offs, p):
+    codes = O.encode(bytes(res))
+
+    def cb(pairs, ro, co):
+        out = O.batch(mode, codes, offs, codes, offs, pairs, p, bl_roff=ro, bl_coff=co,
+                      nthreads=2)
+        return out["score_aln"]
+    return cb
+
+
+@pytest.mark.parametrize("batch_sz", [1, 7, 50, 299, 300, 10 ** 10])
+def test_batches_and_prunes_xdrop(native, oracle_mod, batch_sz):
+    from pastis_gb300 import capi
+    O = oracle_mod
+    res, offs, rows, cols, rng = _block()
+    vals = np.zeros(len(rows), dtype=capi.KMERLOC_DTYPE)
+    vals["count"] = rng.integers(1, 4, len(rows))
+    vals["score"] = rng.integers(-1, 30, len(rows))
+    L = np.diff(offs).astype(int)
+    vals["first_r"] = [rng.integers(0, L[r] - 6) for r in rows]
+    vals["first_c"] = [rng.integers(0, L[c] - 6) for c in cols]
+    vals["score_aln"] = 0.5  # stale values must be overwritten
+    p = O.make_params(gap_first=-2, gap_ext=-11, xdrop_gap=-11)
+    ckthr, mosthr = 1, 3.0
+    r2, c2, v2, st = capi.pw_aln_batch(capi.MODE_XDROP, rows, cols, vals, res, offs,
+                                      batch_sz=batch_sz, ckthr=ckthr, mosthr=mosthr,
+                                      callback=_oracle_cb(O, 1, res, offs, p))
+    keep = ~((vals["count"] <= ckthr) | (vals["score"] <= mosthr))
+    assert st["nnz_in"] == len(rows) and st["nnz_kmer_thr"] == keep.sum()
+    n = int(keep.sum())
+    assert st["batches"] == n // min(batch_sz, 10 ** 10) + 1
+    assert st["empty_batches"] == (1 if n % batch_sz == 0 else 0)
+    # expected: oracle on the kept entries, then drop score_aln == 0
+    pr = np.zeros(n, dtype=O.PAIR_DTYPE)
+    pr["row"], pr["col"] = rows[keep], cols[keep]
+    pr["rs0"], pr["cs0"] = vals["first_r"][keep], vals["first_c"][keep]
+    pr["count"] = vals["count"][keep]
+    exp = O.batch(1, O.encode(bytes(res)), offs, O.encode(bytes(res)), offs, pr, p)
+    ok = exp["score_aln"] != 0
+    assert st["nnz_aln"] == ok.sum()
+    assert (r2 == rows[keep][ok]).all() and (c2 == cols[keep][ok]).all()
+    assert (v2["score_aln"] == exp["score_aln"][ok]).all()
+
+
+def test_sw_block_offsets(native, oracle_mod):
+    """bl_roffset / bl_coffset shift the sequence indices (PWAlign.hpp:47-52)."""
+    from pastis_gb300 import capi
+    O = oracle_mod
+    res, offs, rows, cols, rng = _block(seed=2)
+    rows = rows % 10
+    cols = cols % 10
+    vals = np.zeros(len(rows), dtype=capi.KMERLIGHT_DTYPE)
+    vals["count"] = 2
+    p = O.make_params()
+    r2, c2, v2, st = capi.pw_aln_batch(capi.MODE_SW, rows, cols, vals, res, offs, bl_roff=20,
+                                      bl_coff=25, batch_sz=64,
+                                      callback=_oracle_cb(O, 0, res, offs, p))
+    pr = np.zeros(len(rows), dtype=O.PAIR_DTYPE)
+    pr["row"], pr["col"] = rows, cols
+    exp = O.batch(0, O.encode(bytes(res)), offs, O.encode(bytes(res)), offs, pr, p, bl_roff=20,
+                  bl_coff=25)
+    ok = exp["score_aln"] != 0
+    assert st["nnz_aln"] == ok.sum()
+    assert (v2["score_aln"] == exp["score_aln"][ok]).all()
+
+
+def test_empty_block(native):
+    from pastis_gb300 import capi
+    res = np.frombuffer(b"ACDEFG", dtype=np.uint8)
+    offs = np.array([0, 6], dtype=np.uint64)
+    called = []
+    r2, c2, v2, st = capi.pw_aln_batch(capi.MODE_SW, [], [], np.zeros(0, capi.KMERLIGHT_DTYPE),
+                                      res, offs, callback=lambda *a: called.append(1))
+    assert st["nnz_in"] == 0 and st["batches"] == 0 and not called
