@@ -204,7 +204,9 @@ def run_gpu(args, rank, world, local_rank):
     ctx.set_seqs(0, w.ascii, w.offs)
     ctx.share_row_seqs()
 
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: the kernels and the timing events must share it
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
     d_pairs = torch.from_numpy(w.pairs.view(np.uint8).copy()).to(f"cuda:{dev}")
     d_out = torch.empty(n * capi.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{dev}")
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{dev}")

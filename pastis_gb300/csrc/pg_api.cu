@@ -111,19 +111,24 @@ struct pg_ctx {
     int8_t *d_sm = nullptr;
     cudaStream_t stream = nullptr;
     int nsm = 0;
-    int grid = 0;                  // persistent blocks
+    int grid = 0;                  // persistent blocks of the warp-per-pair kernel
+    int grid_xd = 0;               // persistent blocks of k_xd
+    int grid_wide = 0;             // blocks of k_xd_wide
     Side side[2];
     bool cols_share_rows = false;
     // scratch
-    unsigned int *d_counter = nullptr;
+    unsigned int *d_counter = nullptr;  // 3 work counters
     int *d_status = nullptr;
     unsigned long long *d_exec = nullptr;
-    pg::Edge *d_bnd = nullptr;
-    uint64_t bnd_stride = 0;
+    void *d_bnd = nullptr;              // per-warp DP row scratch
+    uint64_t bnd_bytes = 0;             // bytes per warp
     size_t bnd_warps = 0;
-    int *d_gring = nullptr;
+    int *d_gring = nullptr;             // per-warp X-drop fallback ring
     int gring_w = 0;
     size_t gring_warps = 0;
+    pg::XdRec *d_xd = nullptr;          // 2 extension records per pair
+    uint32_t *d_ovf = nullptr;          // overflowed extension tasks
+    uint64_t xd_cap = 0;
     // staging for the host-buffer entry point
     pg_pair *d_pairs = nullptr;
     pg_result *d_out = nullptr;
@@ -187,6 +192,8 @@ void pg_destroy(pg_ctx *ctx)
     cudaFree(ctx->d_exec);
     cudaFree(ctx->d_bnd);
     cudaFree(ctx->d_gring);
+    cudaFree(ctx->d_xd);
+    cudaFree(ctx->d_ovf);
     cudaFree(ctx->d_pairs);
     cudaFree(ctx->d_out);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -236,18 +243,23 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     CUD(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CUD(cudaMalloc(&c->d_sm, sizeof c->sm));
     CUD(cudaMemcpy(c->d_sm, c->sm, sizeof c->sm, cudaMemcpyHostToDevice));
-    CUD(cudaMalloc(&c->d_counter, sizeof(unsigned int)));
+    CUD(cudaMalloc(&c->d_counter, 4 * sizeof(unsigned int)));
     CUD(cudaMalloc(&c->d_status, sizeof(int)));
     CUD(cudaMalloc(&c->d_exec, sizeof(unsigned long long)));
     CUD(cudaMemset(c->d_exec, 0, sizeof(unsigned long long)));
     CUD(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, cfg->device));
     int per_sm = 0;
-    if (cfg->mode == PG_MODE_XDROP)
-        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pg::k_xdrop<0>, pg::WARPS * 32, 0));
-    else
+    if (cfg->mode == PG_MODE_XDROP) {
+        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pg::k_ga<0>, pg::WARPS * 32, 0));
+        int px = 0, pw = 0;
+        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&px, pg::k_xd, pg::XT, 0));
+        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pw, pg::k_xd_wide, pg::WARPS * 32, 0));
+        c->grid_xd = c->nsm * std::max(px, 1);
+        c->grid_wide = c->nsm * std::max(pw, 1);
+    } else {
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pg::k_sw<0>, pg::WARPS * 32, 0));
-    if (per_sm < 1) per_sm = 1;
-    c->grid = c->nsm * per_sm;
+    }
+    c->grid = c->nsm * std::max(per_sm, 1);
 #undef CUD
     *out = c;
     return PG_OK;
@@ -258,31 +270,47 @@ static int ensure_scratch(pg_ctx *c)
 {
     const uint32_t rmax = c->side[0].maxlen;
     const uint32_t cmax = c->cols_share_rows ? rmax : c->side[1].maxlen;
-    const uint64_t stride = (uint64_t)cmax + 1;
+    // one DP row of the widest edge type (local statistics, 3 words)
+    const size_t per_warp = ((size_t)cmax + 1) * sizeof(pg::Edge<pg::L2>);
     // keep the row scratch within 8 GiB: fewer resident warps for very long sequences
-    const size_t want_warps = (size_t)c->grid * pg::WARPS;
-    size_t warps = want_warps;
-    const size_t per_warp = stride * sizeof(pg::Edge);
+    size_t warps = (size_t)c->grid * pg::WARPS;
     const size_t budget = (size_t)8 << 30;
     if (per_warp * warps > budget) {
         warps = std::max<size_t>(pg::WARPS, budget / per_warp / pg::WARPS * pg::WARPS);
         c->grid = (int)(warps / pg::WARPS);
     }
-    if (stride > c->bnd_stride || warps > c->bnd_warps || !c->d_bnd) {
+    if (per_warp > c->bnd_bytes || warps > c->bnd_warps || !c->d_bnd) {
         cudaFree(c->d_bnd);
         c->d_bnd = nullptr;
+        c->bnd_bytes = 0;
         CU(cudaMalloc(&c->d_bnd, per_warp * warps));
-        c->bnd_stride = stride;
+        c->bnd_bytes = per_warp;
         c->bnd_warps = warps;
     }
-    const int gw = (int)next_pow2((size_t)std::max(rmax, cmax) + 4);
-    if (gw > c->gring_w || warps > c->gring_warps || !c->d_gring) {
-        cudaFree(c->d_gring);
-        c->d_gring = nullptr;
-        CU(cudaMalloc(&c->d_gring, (size_t)3 * gw * sizeof(int) * warps));
-        c->gring_w = gw;
-        c->gring_warps = warps;
+    if (c->cfg.mode == PG_MODE_XDROP) {
+        const int gw = (int)next_pow2((size_t)std::max(rmax, cmax) + 4);
+        const size_t wwarps = (size_t)c->grid_wide * pg::WARPS;
+        if (gw > c->gring_w || wwarps > c->gring_warps || !c->d_gring) {
+            cudaFree(c->d_gring);
+            c->d_gring = nullptr;
+            c->gring_w = 0;
+            CU(cudaMalloc(&c->d_gring, (size_t)3 * gw * sizeof(int) * wwarps));
+            c->gring_w = gw;
+            c->gring_warps = wwarps;
+        }
     }
+    return PG_OK;
+}
+
+// per-pair X-drop scratch for a batch of n pairs
+static int ensure_batch(pg_ctx *c, uint64_t n)
+{
+    if (c->cfg.mode != PG_MODE_XDROP || n <= c->xd_cap) return PG_OK;
+    cudaFree(c->d_xd); cudaFree(c->d_ovf);
+    c->d_xd = nullptr; c->d_ovf = nullptr; c->xd_cap = 0;
+    CU(cudaMalloc(&c->d_xd, 2 * n * sizeof(pg::XdRec)));
+    CU(cudaMalloc(&c->d_ovf, 2 * n * sizeof(uint32_t)));
+    c->xd_cap = n;
     return PG_OK;
 }
 
@@ -351,21 +379,29 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
     kp.go = c->go; kp.ge = c->ge; kp.xg = c->xg; kp.xdrop = c->cfg.xdrop;
     kp.seed_len = c->cfg.seed_len; kp.seed_count = c->cfg.seed_count; kp.flags = c->cfg.flags;
     kp.ani_thr = c->cfg.ani_thr; kp.cov_thr = c->cfg.cov_thr;
+    int rc = ensure_batch(c, n);
+    if (rc) return rc;
     kp.counter = c->d_counter; kp.status = c->d_status; kp.exec_cells = c->d_exec;
-    kp.bnd = c->d_bnd; kp.bnd_stride = c->bnd_stride;
+    kp.xd = c->d_xd; kp.ovf = c->d_ovf;
+    kp.bnd = c->d_bnd; kp.bnd_bytes = c->bnd_bytes;
     kp.gring = c->d_gring; kp.gring_w = c->gring_w;
-    CU(cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned int), st));
+    CU(cudaMemsetAsync(c->d_counter, 0, 4 * sizeof(unsigned int), st));
     CU(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
     const uint64_t need_blocks = (n + pg::WARPS - 1) / pg::WARPS;
     const int grid = (int)std::min<uint64_t>((uint64_t)c->grid, need_blocks);
     const dim3 blk(pg::WARPS * 32);
     if (c->cfg.mode == PG_MODE_XDROP) {
+        const uint64_t need_xd = (2 * n + pg::XT - 1) / pg::XT;
+        const int gx = (int)std::min<uint64_t>((uint64_t)c->grid_xd, need_xd);
+        pg::k_xd<<<gx, pg::XT, 0, st>>>(kp);
+        pg::k_xd_wide<<<c->grid_wide, blk, 0, st>>>(kp);
         switch (c->cfg.tie) {
-        case 0: pg::k_xdrop<0><<<grid, blk, 0, st>>>(kp); break;
-        case 1: pg::k_xdrop<1><<<grid, blk, 0, st>>>(kp); break;
-        case 2: pg::k_xdrop<2><<<grid, blk, 0, st>>>(kp); break;
-        default: pg::k_xdrop<3><<<grid, blk, 0, st>>>(kp); break;
+        case 0: pg::k_ga<0><<<grid, blk, 0, st>>>(kp); break;
+        case 1: pg::k_ga<1><<<grid, blk, 0, st>>>(kp); break;
+        case 2: pg::k_ga<2><<<grid, blk, 0, st>>>(kp); break;
+        default: pg::k_ga<3><<<grid, blk, 0, st>>>(kp); break;
         }
+        c->last_launches = 3;
     } else {
         switch (c->cfg.tie) {
         case 0: pg::k_sw<0><<<grid, blk, 0, st>>>(kp); break;
@@ -373,9 +409,9 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         case 2: pg::k_sw<2><<<grid, blk, 0, st>>>(kp); break;
         default: pg::k_sw<3><<<grid, blk, 0, st>>>(kp); break;
         }
+        c->last_launches = 1;
     }
     CU(cudaGetLastError());
-    c->last_launches = 1;
     return PG_OK;
 }
 

@@ -1,10 +1,21 @@
 // pg_kernels.cuh -- batch kernels behind pg_align (sm_103a).
 //
-// Persistent, work-stealing launch: a grid sized to the resident capacity of
-// the GPU; each warp takes the next pair index from a device counter until the
-// batch is done, so pairs of very different lengths balance themselves.  Each
-// pair is finished inside one warp (extension, alignment, statistics, filter),
-// so no intermediate result leaves the SM.
+// --sxa (X-drop), three launches per batch:
+//   k_xd       one thread per (pair, seed): both X-drop directions on a
+//              16-slot per-thread ring in shared memory (the band of the
+//              default gap model never spans more than 13 columns); threads
+//              take the next (pair, seed) from a device counter, so long and
+//              short extensions balance.  Writes the extended region.
+//   k_xd_wide  one warp per (pair, seed) whose band outgrew the thread ring:
+//              256-slot shared ring, per-warp global ring beyond that.
+//   k_ga       one warp per pair: global alignment with statistics over each
+//              seed's region (a region equal to the first seed's is not
+//              realigned: an equal identity never replaces the kept one),
+//              best identity, coverage/ANI filter, result record.
+// --sfa (SW): k_sw, one warp per pair, local alignment with statistics.
+//
+// All kernels are persistent with work stealing (grids sized to the resident
+// capacity) so pairs of very different lengths balance themselves.
 #pragma once
 #include <cstdint>
 
@@ -14,11 +25,26 @@
 
 namespace pg {
 
-constexpr int WARPS = 8;          // warps per block
-constexpr int RING_W = 256;       // shared-memory X-drop ring (ints per anti-diagonal)
+constexpr int WARPS = 8;          // warps per block (k_ga, k_sw, k_xd_wide)
+constexpr int RING_W = 256;       // shared ring per warp in k_xd_wide
+constexpr int XT = 128;           // threads per block in k_xd
+constexpr int XW = 16;            // per-thread ring slots in k_xd
 
 // status word bits (read back by the host after a batch)
 constexpr int ST_BAD_INDEX = 1;
+
+// extension of one (pair, seed)
+constexpr uint32_t XF_NONE = 1;    // seed not tried (seed_count / spurious switch)
+constexpr uint32_t XF_SAME = 2;    // same seed as the first one
+constexpr uint32_t XF_BAD = 4;     // seed clamped at a sequence end
+constexpr uint32_t XF_OVF = 8;     // band outgrew the thread ring: redo in k_xd_wide
+constexpr uint32_t XF_BADIDX = 16; // pair index out of range
+
+struct XdRec {
+    uint16_t bv, ev, bh, eh;
+    uint32_t cells;
+    uint32_t flags;
+};
 
 struct KParams {
     const pg_pair *pairs;
@@ -30,11 +56,13 @@ struct KParams {
     const int8_t *sm;             // 25 x 25
     int go, ge, xg, xdrop, seed_len, seed_count, flags, ani_thr;
     double cov_thr;
-    unsigned int *counter;        // work counter (zeroed before launch)
+    unsigned int *counter;        // [0] k_ga / k_sw pairs, [1] k_xd tasks, [2] overflow count
     int *status;                  // error bits
     unsigned long long *exec_cells; // cells actually computed (whole batch)
-    Edge *bnd;                    // per-warp row scratch, bnd_stride entries each
-    uint64_t bnd_stride;
+    XdRec *xd;                    // 2 per pair
+    uint32_t *ovf;                // overflowed (pair, seed) tasks
+    void *bnd;                    // per-warp row scratch
+    uint64_t bnd_bytes;           // bytes per warp
     int *gring;                   // per-warp fallback ring, 3 * gring_w ints each
     int gring_w;
 };
@@ -49,13 +77,13 @@ __device__ __forceinline__ void load_sm(int *ssm, const int8_t *sm)
 
 __device__ __forceinline__ uint32_t sat_u32(uint64_t x) { return x > 0xffffffffull ? 0xffffffffu : (uint32_t)x; }
 
-// identity exactly as computeAlignmentStats forms it, then the coverage/ANI
-// filter of SeqanFullAligner.cpp:247-260 / SeqanXdropAligner.cpp:337-352
+// identity exactly as computeAlignmentStats forms it
 __device__ __forceinline__ float identity_of(uint32_t M, uint32_t L)
 {
     return (float)((100.0 * (double)M) / (double)L);
 }
 
+// coverage/ANI filter of SeqanFullAligner.cpp:247-260 / SeqanXdropAligner.cpp:337-352
 __device__ __forceinline__ void apply_filter(pg_result &o, int len_r, int len_c, double cov_thr, int ani_thr)
 {
     const double a = (double)o.aln_len - (double)o.gap_opens;
@@ -69,76 +97,112 @@ __device__ __forceinline__ void apply_filter(pg_result &o, int len_r, int len_c,
     }
 }
 
-__device__ __forceinline__ bool fetch_task(const KParams &kp, uint64_t &task)
+__device__ __forceinline__ pg_result empty_result()
 {
-    const int lane = threadIdx.x & 31;
-    unsigned int t = 0;
-    if (lane == 0) t = atomicAdd(kp.counter, 1u);
-    t = __shfl_sync(FULL, t, 0);
-    task = t;
-    return task < kp.n;
+    pg_result o;
+    o.score = 0; o.aln_len = 0; o.matches = 0; o.gap_opens = 0;
+    o.beg_h = o.end_h = o.beg_v = o.end_v = 0;
+    o.identity = 0.0f; o.score_aln = 0.0f; o.seed_used = 0; o.flags = PG_RF_EMPTY;
+    o.pad = 0; o.cells = 0;
+    return o;
 }
 
-// resolve a pair's sequences; false (and a status bit) on a bad index
+__device__ __forceinline__ bool warp_fetch(unsigned int *counter, uint64_t n, uint64_t &task)
+{
+    unsigned int t = 0;
+    if ((threadIdx.x & 31) == 0) t = atomicAdd(counter, 1u);
+    t = __shfl_sync(FULL, t, 0);
+    task = t;
+    return task < n;
+}
+
+// a pair's sequences; false on a bad index
 __device__ __forceinline__ bool pair_seqs(const KParams &kp, const pg_pair &pr,
                                           const uint8_t *&V, int &m, const uint8_t *&Hs, int &n)
 {
     const uint64_t r = (uint64_t)pr.row + kp.roff, c = (uint64_t)pr.col + kp.coff;
-    if (r >= kp.nr || c >= kp.nc) {
-        if ((threadIdx.x & 31) == 0) atomicOr(kp.status, ST_BAD_INDEX);
-        return false;
-    }
+    if (r >= kp.nr || c >= kp.nc) return false;
     const uint64_t r0 = kp.roffs[r], c0 = kp.coffs[c];
     V = kp.rseq + r0; m = (int)(kp.roffs[r + 1] - r0);
     Hs = kp.cseq + c0; n = (int)(kp.coffs[c + 1] - c0);
     return true;
 }
 
-// --------------------------------------------------------------- --sfa (SW)
-template <int TIE>
-__global__ void __launch_bounds__(WARPS * 32) k_sw(const KParams kp)
+// seed s of a pair as a region [bv, ev) x [bh, eh), clamped at sequence ends
+__device__ __forceinline__ bool seed_region(const KParams &kp, const pg_pair &pr, int s, int m, int n,
+                                            int &bv, int &ev, int &bh, int &eh)
 {
-    __shared__ int ssm[32 * 32];
-    load_sm(ssm, kp.sm);
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const uint64_t gw = (uint64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
-    Edge *bnd = kp.bnd + gw * kp.bnd_stride;
-    unsigned long long exec = 0;
-    uint64_t task;
-    while (fetch_task(kp, task)) {
-        const pg_pair pr = kp.pairs[task];
-        const uint8_t *V, *Hs;
-        int m, n;
-        pg_result o;
-        o.score = 0; o.aln_len = 0; o.matches = 0; o.gap_opens = 0;
-        o.beg_h = o.end_h = o.beg_v = o.end_v = 0;
-        o.identity = 0.0f; o.score_aln = 0.0f; o.seed_used = 0; o.flags = PG_RF_EMPTY;
-        o.pad = 0; o.cells = 0;
-        if (pair_seqs(kp, pr, V, m, Hs, n)) {
-            const DpOut d = dp_dispatch<true, TIE>(V, m, Hs, n, ssm, kp.go, kp.ge, bnd);
-            exec += (unsigned long long)m * (unsigned long long)n;
-            o.cells = sat_u32((uint64_t)m * (uint64_t)n);
-            if (d.have) {
-                const uint32_t D = d.st.md >> 16, M = d.st.md & 0xffffu;
-                const int i0 = (int)(d.st.b & 0xffffu), j0 = (int)(d.st.b >> 16);
-                const uint32_t L = (uint32_t)((d.ei - i0) + (d.ej - j0)) - D;
-                o.score = d.score;
-                o.aln_len = L; o.matches = M; o.gap_opens = d.st.g;
-                o.beg_v = (uint16_t)i0; o.end_v = (uint16_t)d.ei;
-                o.beg_h = (uint16_t)j0; o.end_h = (uint16_t)d.ej;
-                if (L == 0) { o.identity = 0.0f; }
-                else { o.identity = identity_of(M, L); o.flags = 0; }
-            }
-            apply_filter(o, m, n, kp.cov_thr, kp.ani_thr);
-        }
-        if (lane == 0) kp.out[task] = o;
+    const int r0 = s == 0 ? pr.rs0 : pr.rs1;
+    const int c0 = s == 0 ? pr.cs0 : pr.cs1;
+    bv = r0; ev = r0 + kp.seed_len; bh = c0; eh = c0 + kp.seed_len;
+    if (ev > m || eh > n) {
+        bv = min(bv, m); ev = min(ev, m); bh = min(bh, n); eh = min(eh, n);
+        return true;
     }
-    if (lane == 0 && exec) atomicAdd(kp.exec_cells, exec);
+    return false;
 }
 
-// --------------------------------------------------------------- --sxa
-// one direction of X-drop, shared ring first, per-warp global ring on overflow
+// ------------------------------------------------------------------ k_xd
+__global__ void __launch_bounds__(XT) k_xd(const KParams kp)
+{
+    __shared__ int ssm[32 * 32];
+    __shared__ int ring[3 * XW * XT];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
+    int *base = ring + threadIdx.x;
+    const uint64_t ntask = 2 * kp.n;
+    unsigned long long exec = 0;
+    for (;;) {
+        const uint64_t task = atomicAdd(&kp.counter[1], 1u);
+        if (task >= ntask) break;
+        const uint64_t p = task >> 1;
+        const int s = (int)(task & 1);
+        const pg_pair pr = kp.pairs[p];
+        XdRec rec{0, 0, 0, 0, 0u, 0u};
+        const uint8_t *V, *Hs;
+        int m, n;
+        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
+            rec.flags = XF_BADIDX;
+        } else if (s >= kp.seed_count ||
+                   (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
+            rec.flags = XF_NONE;
+        } else if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
+            rec.flags = XF_SAME;
+        } else {
+            int bv, ev, bh, eh;
+            if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
+            bool ok = true;
+            if (bv > 0 && bh > 0) {
+                const XdOut x = xdrop_dir_thread<XW, XT>(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1,
+                                                         ssm, kp.xg, kp.xdrop, base);
+                ok = x.ok;
+                rec.cells += x.cells;
+                bv -= x.dv; bh -= x.dh;
+            }
+            if (ok && ev < m && eh < n) {
+                const XdOut x = xdrop_dir_thread<XW, XT>(V + ev, m - ev, 1, Hs + eh, n - eh, 1,
+                                                         ssm, kp.xg, kp.xdrop, base);
+                ok = x.ok;
+                rec.cells += x.cells;
+                ev += x.dv; eh += x.dh;
+            }
+            if (ok) {
+                rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev;
+                rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
+                exec += rec.cells;
+            } else {
+                rec.flags |= XF_OVF;
+                rec.cells = 0;
+                const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
+                kp.ovf[slot] = (uint32_t)task;
+            }
+        }
+        kp.xd[task] = rec;
+    }
+    if (exec) atomicAdd(kp.exec_cells, exec);
+}
+
+// ------------------------------------------------------------- k_xd_wide
 __device__ __forceinline__ XdOut xdrop_dir_any(const uint8_t *V, int nv, int vstep,
                                                const uint8_t *Hs, int nh, int hstep,
                                                const int *ssm, int g, int X, int *sring,
@@ -149,8 +213,7 @@ __device__ __forceinline__ XdOut xdrop_dir_any(const uint8_t *V, int nv, int vst
     return o;
 }
 
-template <int TIE>
-__global__ void __launch_bounds__(WARPS * 32) k_xdrop(const KParams kp)
+__global__ void __launch_bounds__(WARPS * 32) k_xd_wide(const KParams kp)
 {
     __shared__ int ssm[32 * 32];
     __shared__ int sring[WARPS][3 * RING_W];
@@ -158,85 +221,172 @@ __global__ void __launch_bounds__(WARPS * 32) k_xdrop(const KParams kp)
     __syncthreads();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint64_t gw = (uint64_t)blockIdx.x * WARPS + wib;
-    Edge *bnd = kp.bnd + gw * kp.bnd_stride;
+    const uint64_t nw = (uint64_t)gridDim.x * WARPS;
     int *gring = kp.gring + gw * 3ull * (uint64_t)kp.gring_w;
-    int *ring = sring[wib];
+    const unsigned int novf = kp.counter[2];
     unsigned long long exec = 0;
-    uint64_t task;
-    while (fetch_task(kp, task)) {
-        const pg_pair pr = kp.pairs[task];
+    for (uint64_t q = gw; q < novf; q += nw) {
+        const uint32_t task = kp.ovf[q];
+        const uint64_t p = task >> 1;
+        const int s = (int)(task & 1);
+        const pg_pair pr = kp.pairs[p];
         const uint8_t *V, *Hs;
         int m, n;
-        pg_result best;
-        best.score = 0; best.aln_len = 0; best.matches = 0; best.gap_opens = 0;
-        best.beg_h = best.end_h = best.beg_v = best.end_v = 0;
-        best.identity = 0.0f; best.score_aln = 0.0f; best.seed_used = 0;
-        best.flags = PG_RF_EMPTY; best.pad = 0; best.cells = 0;
-        if (pair_seqs(kp, pr, V, m, Hs, n)) {
-            uint64_t cells = 0;
-            bool have = false, badseed = false;
-            int prev_r0 = -1, prev_c0 = -1, pbv = 0, pev = 0, pbh = 0, peh = 0;
-            uint32_t prev_xcells = 0;
-            for (int cnt = 0; cnt < kp.seed_count && cnt < 2; ++cnt) {
-                if (cnt > 0 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2) break;
-                const int r0 = cnt == 0 ? pr.rs0 : pr.rs1;
-                const int c0 = cnt == 0 ? pr.cs0 : pr.cs1;
-                int bv = r0, ev = r0 + kp.seed_len, bh = c0, eh = c0 + kp.seed_len;
-                if (ev > m || eh > n) {
-                    badseed = true;
-                    bv = min(bv, m); ev = min(ev, m); bh = min(bh, n); eh = min(eh, n);
-                }
-                uint32_t xcells = 0;
-                if (cnt > 0 && r0 == prev_r0 && c0 == prev_c0) {
-                    // the same seed again: same extension, same alignment; an
-                    // equal identity never replaces the kept one
-                    cells += prev_xcells + (uint64_t)(pev - pbv) * (uint64_t)(peh - pbh);
-                    continue;
-                }
-                if (bv > 0 && bh > 0) {
-                    XdOut x = xdrop_dir_any(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1, ssm, kp.xg,
-                                            kp.xdrop, ring, gring, kp.gring_w);
-                    xcells += x.cells;
-                    bv -= x.dv; bh -= x.dh;
-                }
-                if (ev < m && eh < n) {
-                    XdOut x = xdrop_dir_any(V + ev, m - ev, 1, Hs + eh, n - eh, 1, ssm, kp.xg,
-                                            kp.xdrop, ring, gring, kp.gring_w);
-                    xcells += x.cells;
-                    ev += x.dv; eh += x.dh;
-                }
-                exec += xcells;
-                const uint64_t area = (uint64_t)(ev - bv) * (uint64_t)(eh - bh);
-                cells += xcells + area;
-                const bool same_region = cnt > 0 && bv == pbv && ev == pev && bh == pbh && eh == peh;
-                prev_r0 = r0; prev_c0 = c0; prev_xcells = xcells;
-                pbv = bv; pev = ev; pbh = bh; peh = eh;
-                if (same_region) continue;   // identical alignment, cannot win
-                const DpOut d = dp_dispatch<false, TIE>(V + bv, ev - bv, Hs + bh, eh - bh, ssm,
-                                                        kp.go, kp.ge, bnd);
-                exec += area;
-                const uint32_t D = d.st.md >> 16, M = d.st.md & 0xffffu;
-                const uint32_t L = (uint32_t)((ev - bv) + (eh - bh)) - D;
-                pg_result cur;
-                cur.score = d.score; cur.aln_len = L; cur.matches = M; cur.gap_opens = d.st.g;
-                cur.beg_v = (uint16_t)bv; cur.end_v = (uint16_t)ev;
-                cur.beg_h = (uint16_t)bh; cur.end_h = (uint16_t)eh;
-                cur.seed_used = (uint8_t)cnt; cur.pad = 0; cur.cells = 0; cur.score_aln = 0.0f;
-                if (L == 0) { cur.identity = 0.0f; cur.flags = PG_RF_EMPTY; }
-                else { cur.identity = identity_of(M, L); cur.flags = 0; }
-                // an empty alignment (identity 0/0) never replaces or is replaced
-                const bool cur_nan = (cur.flags & PG_RF_EMPTY) != 0;
-                const bool best_nan = (best.flags & PG_RF_EMPTY) != 0;
-                if (!have || (!cur_nan && !best_nan && cur.identity > best.identity)) {
-                    best = cur;
-                    have = true;
-                }
-            }
-            best.cells = sat_u32(cells);
-            if (badseed) best.flags |= PG_RF_BAD_SEED;
-            apply_filter(best, m, n, kp.cov_thr, kp.ani_thr);
+        pair_seqs(kp, pr, V, m, Hs, n);
+        XdRec rec{0, 0, 0, 0, 0u, 0u};
+        int bv, ev, bh, eh;
+        if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
+        if (bv > 0 && bh > 0) {
+            const XdOut x = xdrop_dir_any(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1, ssm, kp.xg,
+                                          kp.xdrop, sring[wib], gring, kp.gring_w);
+            rec.cells += x.cells;
+            bv -= x.dv; bh -= x.dh;
         }
-        if (lane == 0) kp.out[task] = best;
+        if (ev < m && eh < n) {
+            const XdOut x = xdrop_dir_any(V + ev, m - ev, 1, Hs + eh, n - eh, 1, ssm, kp.xg,
+                                          kp.xdrop, sring[wib], gring, kp.gring_w);
+            rec.cells += x.cells;
+            ev += x.dv; eh += x.dh;
+        }
+        rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev; rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
+        exec += rec.cells;
+        if (lane == 0) kp.xd[task] = rec;
+    }
+    if (lane == 0 && exec) atomicAdd(kp.exec_cells, exec);
+}
+
+// ------------------------------------------------------------------ k_ga
+// stripe height by region height; the one-word statistics go up to 8 rows per
+// lane, the wider ones stop at 4 to stay within the register budget
+template <class S, int TIE>
+__device__ __forceinline__ DpOut<S> dp_dispatch(const uint8_t *V, int m, const uint8_t *Hs, int n,
+                                                const int *ssm, int go, int ge, void *bnd)
+{
+    Edge<S> *b = (Edge<S> *)bnd;
+    constexpr bool WIDE = sizeof(S) > 4;
+    if (m <= 64) return dp_warp<S, TIE, 2>(V, m, Hs, n, ssm, go, ge, b);
+    if (m <= 128 || WIDE) return dp_warp<S, TIE, 4>(V, m, Hs, n, ssm, go, ge, b);
+    return dp_warp<S, TIE, WIDE ? 4 : 8>(V, m, Hs, n, ssm, go, ge, b);
+}
+
+template <int TIE>
+__global__ void __launch_bounds__(WARPS * 32, 2) k_ga(const KParams kp)
+{
+    __shared__ int ssm[32 * 32];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint64_t gw = (uint64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    void *bnd = (char *)kp.bnd + gw * kp.bnd_bytes;
+    unsigned long long exec = 0;
+    uint64_t p;
+    while (warp_fetch(&kp.counter[0], kp.n, p)) {
+        const pg_pair pr = kp.pairs[p];
+        const uint8_t *V, *Hs;
+        int m, n;
+        pg_result best = empty_result();
+        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
+            if (lane == 0) { atomicOr(kp.status, ST_BAD_INDEX); kp.out[p] = best; }
+            continue;
+        }
+        uint64_t cells = 0;
+        bool have = false, bad = false;
+        XdRec r0{0, 0, 0, 0, 0u, XF_NONE};
+        for (int s = 0; s < 2; ++s) {
+            XdRec rec = kp.xd[2 * p + s];
+            if (rec.flags & XF_NONE) continue;
+            if (rec.flags & XF_SAME) {
+                // the same extension and alignment again
+                cells += (uint64_t)r0.cells + (uint64_t)(r0.ev - r0.bv) * (uint64_t)(r0.eh - r0.bh);
+                continue;
+            }
+            if (rec.flags & XF_BAD) bad = true;
+            const int bv = rec.bv, ev = rec.ev, bh = rec.bh, eh = rec.eh;
+            const uint64_t area = (uint64_t)(ev - bv) * (uint64_t)(eh - bh);
+            cells += rec.cells + area;
+            const bool same_region = s == 1 && !(r0.flags & XF_NONE) && bv == r0.bv &&
+                                     ev == r0.ev && bh == r0.bh && eh == r0.eh;
+            if (s == 0) r0 = rec;
+            if (same_region) continue;  // identical alignment, cannot win
+            const int rm = ev - bv, rn = eh - bh;
+            int score;
+            uint32_t M, D, G;
+            if (rm <= S1::MAXSIDE && rn <= S1::MAXSIDE) {
+                const DpOut<S1> d = dp_dispatch<S1, TIE>(V + bv, rm, Hs + bh, rn, ssm, kp.go, kp.ge, bnd);
+                score = d.score; M = d.st.M(); D = d.st.D(); G = d.st.G();
+            } else {
+                const DpOut<S2> d = dp_dispatch<S2, TIE>(V + bv, rm, Hs + bh, rn, ssm, kp.go, kp.ge, bnd);
+                score = d.score; M = d.st.M(); D = d.st.D(); G = d.st.G();
+            }
+            exec += area;
+            const uint32_t L = (uint32_t)(rm + rn) - D;
+            pg_result cur;
+            cur.score = score; cur.aln_len = L; cur.matches = M; cur.gap_opens = G;
+            cur.beg_v = (uint16_t)bv; cur.end_v = (uint16_t)ev;
+            cur.beg_h = (uint16_t)bh; cur.end_h = (uint16_t)eh;
+            cur.seed_used = (uint8_t)s; cur.pad = 0; cur.cells = 0; cur.score_aln = 0.0f;
+            if (L == 0) { cur.identity = 0.0f; cur.flags = PG_RF_EMPTY; }
+            else { cur.identity = identity_of(M, L); cur.flags = 0; }
+            // an empty alignment (identity 0/0) never replaces or is replaced
+            const bool cur_nan = (cur.flags & PG_RF_EMPTY) != 0;
+            const bool best_nan = (best.flags & PG_RF_EMPTY) != 0;
+            if (!have || (!cur_nan && !best_nan && cur.identity > best.identity)) {
+                best = cur;
+                have = true;
+            }
+        }
+        best.cells = sat_u32(cells);
+        if (bad) best.flags |= PG_RF_BAD_SEED;
+        apply_filter(best, m, n, kp.cov_thr, kp.ani_thr);
+        if (lane == 0) kp.out[p] = best;
+    }
+    if (lane == 0 && exec) atomicAdd(kp.exec_cells, exec);
+}
+
+// ------------------------------------------------------------------ k_sw
+template <int TIE>
+__global__ void __launch_bounds__(WARPS * 32) k_sw(const KParams kp)
+{
+    __shared__ int ssm[32 * 32];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint64_t gw = (uint64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    void *bnd = (char *)kp.bnd + gw * kp.bnd_bytes;
+    unsigned long long exec = 0;
+    uint64_t p;
+    while (warp_fetch(&kp.counter[0], kp.n, p)) {
+        const pg_pair pr = kp.pairs[p];
+        const uint8_t *V, *Hs;
+        int m, n;
+        pg_result o = empty_result();
+        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
+            if (lane == 0) { atomicOr(kp.status, ST_BAD_INDEX); kp.out[p] = o; }
+            continue;
+        }
+        exec += (unsigned long long)m * (unsigned long long)n;
+        o.cells = sat_u32((uint64_t)m * (uint64_t)n);
+        int score = 0, have = 0, ei = 0, ej = 0, i0 = 0, j0 = 0;
+        uint32_t M = 0, D = 0, G = 0;
+        if (m <= L1::MAXSIDE && n <= L1::MAXSIDE) {
+            const DpOut<L1> d = dp_dispatch<L1, TIE>(V, m, Hs, n, ssm, kp.go, kp.ge, bnd);
+            score = d.score; have = d.have; ei = d.ei; ej = d.ej;
+            M = d.st.M(); D = d.st.D(); G = d.st.G(); i0 = d.st.i0(); j0 = d.st.j0();
+        } else {
+            const DpOut<L2> d = dp_dispatch<L2, TIE>(V, m, Hs, n, ssm, kp.go, kp.ge, bnd);
+            score = d.score; have = d.have; ei = d.ei; ej = d.ej;
+            M = d.st.M(); D = d.st.D(); G = d.st.G(); i0 = d.st.i0(); j0 = d.st.j0();
+        }
+        if (have) {
+            const uint32_t L = (uint32_t)((ei - i0) + (ej - j0)) - D;
+            o.score = score;
+            o.aln_len = L; o.matches = M; o.gap_opens = G;
+            o.beg_v = (uint16_t)i0; o.end_v = (uint16_t)ei;
+            o.beg_h = (uint16_t)j0; o.end_h = (uint16_t)ej;
+            if (L > 0) { o.identity = identity_of(M, L); o.flags = 0; }
+        }
+        apply_filter(o, m, n, kp.cov_thr, kp.ani_thr);
+        if (lane == 0) kp.out[p] = o;
     }
     if (lane == 0 && exec) atomicAdd(kp.exec_cells, exec);
 }

@@ -156,11 +156,12 @@ def test_edge_cases(native, oracle_mod, mode):
 
 def test_block_offsets_and_separate_columns(sw_small, oracle_mod):
     from pastis_gb300 import capi
+    nseq = len(sw_small.offs) - 1
     pairs = sw_small.pairs[:500].copy()
-    pairs["row"] = pairs["row"] % 1000
-    pairs["col"] = pairs["col"] % 1000
+    pairs["row"] = pairs["row"] % (nseq - 37)
+    pairs["col"] = pairs["col"] % (nseq - 123)
     cfg = capi.config(capi.MODE_SW)
-    got, exp = run_both(0, sw_small, cfg, oracle_mod, pairs=pairs, roff=37, coff=1234,
+    got, exp = run_both(0, sw_small, cfg, oracle_mod, pairs=pairs, roff=37, coff=123,
                         share=False)
     assert_same(got, exp, pairs)
 
