@@ -148,6 +148,29 @@ int pg_last_launches(const pg_ctx *ctx);
  * seed whose extension or alignment repeats the first one's. */
 unsigned long long pg_exec_cells(pg_ctx *ctx);
 
+/* Local alignment (--sfa semantics, cfg->mode must be PG_MODE_SW) for callers
+ * that may not allocate device memory: code inside a stream capture, plugins
+ * whose host framework owns the device allocator, loops that must not touch
+ * the allocator between steps.  No reference counterpart: PASTIS itself never
+ * runs on a GPU.  Nothing is allocated; the caller passes every input and
+ * output as device buffers (sequences as residue codes 0..24 in the order
+ * ARNDCQEGHILKMFPSTWYVBZX*J, offsets of nrows+1 / ncols+1 entries, pairs,
+ * results), and the kernel's scratch (work counter, status, score table, one
+ * DP row per warp) lives in one fixed 32 MiB device array that every GPU
+ * loading the library keeps until the process exits.  max_col_len bounds the
+ * column sequences (at most 65535); a longer one is rejected with
+ * PG_ERR_RANGE.  The first call on a device looks up the array's device
+ * address, so make that first call before any stream capture.  Calls share
+ * the array: two calls that overlap on the GPU (other streams or threads)
+ * race, so serialize them.  Returns after the batch has finished on `stream`
+ * (NULL = the legacy default stream); results equal pg_align's bit for bit. */
+int pg_align_sw_noalloc(const pg_config *cfg,
+                        const uint8_t *d_row_codes, const uint64_t *d_row_offsets, uint64_t nrows,
+                        const uint8_t *d_col_codes, const uint64_t *d_col_offsets, uint64_t ncols,
+                        uint32_t max_col_len, const pg_pair *d_pairs, uint64_t n,
+                        uint64_t bl_roffset, uint64_t bl_coffset, pg_result *d_out,
+                        void *stream);
+
 /* Measured throughput of the DPX add-max instruction on a device, in
  * instructions per second over all SMs (the roofline of the DP kernels). */
 int pg_dpx_peak(int device, double *ops_per_s);

@@ -43,7 +43,7 @@ EXPORTS = {
     "libpastis_gb300.so": ["pg_config_default", "pg_create", "pg_destroy", "pg_set_seqs",
                            "pg_share_row_seqs", "pg_align", "pg_align_device", "pg_sync",
                            "pg_last_launches", "pg_exec_cells", "pg_dpx_peak", "pg_strerror", "pg_last_error",
-                           "pg_version"],
+                           "pg_version", "pg_align_sw_noalloc"],
     "libpastis_synth.so": ["pg_synth_generate", "pg_synth_free", "pg_synth_nseqs",
                            "pg_synth_nres", "pg_synth_npairs", "pg_synth_seq", "pg_synth_offs",
                            "pg_synth_family", "pg_synth_pairs", "pg_synth_homolog",
@@ -94,6 +94,8 @@ def _declare(name, lib):
         lib.pg_exec_cells.argtypes = [vp]
         lib.pg_exec_cells.restype = ctypes.c_ulonglong
         lib.pg_dpx_peak.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
+        lib.pg_align_sw_noalloc.argtypes = [ctypes.POINTER(Config), vp, vp, u64, vp, vp, u64,
+                                            ctypes.c_uint32, vp, u64, u64, u64, vp, vp]
         lib.pg_strerror.argtypes = [i32]
         lib.pg_strerror.restype = ctypes.c_char_p
         lib.pg_last_error.restype = ctypes.c_char_p

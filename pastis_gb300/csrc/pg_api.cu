@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "../../include/pastis_gb300.h"
@@ -534,3 +535,177 @@ unsigned long long pg_exec_cells(pg_ctx *c)
 }
 
 }  // extern "C"
+
+// ------------------------------------------------- no-allocation SW entry point
+//
+// For callers that may not allocate device memory at all: code running inside
+// a stream capture or a driver that owns the whole device pool, plugins
+// embedded in a host framework whose allocator must not be bypassed, or
+// real-time loops that must not touch the allocator between steps.  Instead
+// of a context's cudaMalloc'd scratch, the local-alignment kernel below keeps
+// its work counter, status word, score table and per-warp DP rows in one
+// file-scope device array of fixed size.  Every GPU that loads the library
+// holds that array until the process exits.
+namespace {
+
+constexpr size_t kNoAllocBytes = (size_t)32 << 20;   // PG_NOALLOC_SCRATCH_BYTES
+constexpr size_t kNoAllocHeader = 4096;              // counters, status, score table
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// device address of g_noalloc_scratch per device; filled by the first call on
+// that device (the host-side name of the array is only a stand-in)
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[kMaxDevices] = {};
+
+// k_sw with the per-pair column length checked against the rows it was given
+template <int TIE>
+__global__ void __launch_bounds__(pg::WARPS * 32) k_sw_noalloc(const pg::KParams kp, int max_cols)
+{
+    __shared__ int ssm[32 * 32];
+    pg::load_sm(ssm, kp.sm);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint64_t gw = (uint64_t)blockIdx.x * pg::WARPS + (threadIdx.x >> 5);
+    void *bnd = (char *)kp.bnd + gw * kp.bnd_bytes;
+    unsigned long long exec = 0;
+    uint64_t p;
+    while (pg::warp_fetch(&kp.counter[0], kp.n, p)) {
+        const pg_pair pr = kp.pairs[p];
+        const uint8_t *V, *Hs;
+        int m, n;
+        pg_result o = pg::empty_result();
+        if (!pg::pair_seqs(kp, pr, V, m, Hs, n)) {
+            if (lane == 0) { atomicOr(kp.status, pg::ST_BAD_INDEX); kp.out[p] = o; }
+            continue;
+        }
+        if (n > max_cols || m > 65535) {
+            if (lane == 0) { atomicOr(kp.status, 2); kp.out[p] = o; }
+            continue;
+        }
+        exec += (unsigned long long)m * (unsigned long long)n;
+        o.cells = pg::sat_u32((uint64_t)m * (uint64_t)n);
+        int score = 0, have = 0, ei = 0, ej = 0, i0 = 0, j0 = 0;
+        uint32_t M = 0, D = 0, G = 0;
+        if (m <= pg::L1::MAXSIDE && n <= pg::L1::MAXSIDE) {
+            const pg::DpOut<pg::L1> d = pg::dp_dispatch<pg::L1, TIE>(V, m, Hs, n, ssm, kp.go, kp.ge, bnd);
+            score = d.score; have = d.have; ei = d.ei; ej = d.ej;
+            M = d.st.M(); D = d.st.D(); G = d.st.G(); i0 = d.st.i0(); j0 = d.st.j0();
+        } else {
+            const pg::DpOut<pg::L2> d = pg::dp_dispatch<pg::L2, TIE>(V, m, Hs, n, ssm, kp.go, kp.ge, bnd);
+            score = d.score; have = d.have; ei = d.ei; ej = d.ej;
+            M = d.st.M(); D = d.st.D(); G = d.st.G(); i0 = d.st.i0(); j0 = d.st.j0();
+        }
+        if (have) {
+            const uint32_t L = (uint32_t)((ei - i0) + (ej - j0)) - D;
+            o.score = score;
+            o.aln_len = L; o.matches = M; o.gap_opens = G;
+            o.beg_v = (uint16_t)i0; o.end_v = (uint16_t)ei;
+            o.beg_h = (uint16_t)j0; o.end_h = (uint16_t)ej;
+            if (L > 0) { o.identity = pg::identity_of(M, L); o.flags = 0; }
+        }
+        pg::apply_filter(o, m, n, kp.cov_thr, kp.ani_thr);
+        if (lane == 0) kp.out[p] = o;
+    }
+    if (lane == 0 && exec) atomicAdd(kp.exec_cells, exec);
+}
+
+// restores the caller's current device on every return path
+struct DeviceGuard {
+    int prev = -1;
+    DeviceGuard() { cudaGetDevice(&prev); }
+    ~DeviceGuard() { if (prev >= 0) cudaSetDevice(prev); }
+};
+
+}  // namespace
+
+extern "C" int pg_align_sw_noalloc(const pg_config *cfg,
+                                   const uint8_t *d_row_codes, const uint64_t *d_row_offsets, uint64_t nrows,
+                                   const uint8_t *d_col_codes, const uint64_t *d_col_offsets, uint64_t ncols,
+                                   uint32_t max_col_len, const pg_pair *d_pairs, uint64_t n,
+                                   uint64_t bl_roffset, uint64_t bl_coffset, pg_result *d_out,
+                                   void *stream)
+{
+    if (!cfg) return fail(PG_ERR_ARG, "pg_align_sw_noalloc: null config");
+    int rc = validate(cfg);
+    if (rc) return rc;
+    if (cfg->mode != PG_MODE_SW) return fail(PG_ERR_ARG, "pg_align_sw_noalloc: mode must be PG_MODE_SW");
+    if (n == 0) return PG_OK;
+    if (!d_row_codes || !d_row_offsets || !d_col_codes || !d_col_offsets || !d_pairs || !d_out)
+        return fail(PG_ERR_ARG, "pg_align_sw_noalloc: null buffer");
+    if (n > 0xffffffffull) return fail(PG_ERR_ARG, "pg_align_sw_noalloc: more than 2^32-1 pairs");
+    if (max_col_len > 65535)
+        return fail(PG_ERR_RANGE, "pg_align_sw_noalloc: max_col_len %u above 65535", max_col_len);
+    const size_t per_warp = (((size_t)max_col_len + 1) * sizeof(pg::Edge<pg::L2>) + 255) & ~(size_t)255;
+    const size_t rows_bytes = kNoAllocBytes - kNoAllocHeader;
+    const size_t fit_warps = rows_bytes / per_warp;
+    if (fit_warps < (size_t)pg::WARPS)
+        return fail(PG_ERR_RANGE, "pg_align_sw_noalloc: columns of %u residues need %zu bytes of rows "
+                    "per block, the fixed scratch holds %zu", max_col_len, per_warp * pg::WARPS, rows_bytes);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || cfg->device < 0 || cfg->device >= ndev ||
+        cfg->device >= kMaxDevices)
+        return fail(PG_ERR_NODEV, "pg_align_sw_noalloc: device %d", cfg->device);
+    DeviceGuard guard;
+    CU(cudaSetDevice(cfg->device));
+    unsigned char *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[cfg->device]) {
+            void *ptr = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+            if (e != cudaSuccess || !ptr)
+                return fail(PG_ERR_CUDA, "pg_align_sw_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+            g_noalloc_ptr[cfg->device] = ptr;
+        }
+        base = (unsigned char *)g_noalloc_ptr[cfg->device];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    // header: [0,16) counters, [16,20) status, [24,32) executed cells,
+    // [64, 64+625) score table; DP rows from kNoAllocHeader on
+    int8_t table[PG_NRES * PG_NRES];
+    if (cfg->score_matrix) std::memcpy(table, cfg->score_matrix, sizeof table);
+    else blosum62(table);
+    CU(cudaMemsetAsync(base, 0, 64, st));
+    CU(cudaMemcpyAsync(base + 64, table, sizeof table, cudaMemcpyHostToDevice, st));
+    pg::KParams kp;
+    std::memset(&kp, 0, sizeof kp);
+    kp.pairs = d_pairs; kp.n = n; kp.roff = bl_roffset; kp.coff = bl_coffset;
+    kp.rseq = d_row_codes; kp.roffs = d_row_offsets; kp.nr = nrows;
+    kp.cseq = d_col_codes; kp.coffs = d_col_offsets; kp.nc = ncols;
+    kp.out = d_out; kp.sm = (const int8_t *)(base + 64);
+    if (cfg->gap_semantics == PG_GAPS_AS_CALLED) { kp.go = cfg->gap_ext; kp.ge = cfg->gap_open; }
+    else { kp.go = cfg->gap_open; kp.ge = cfg->gap_ext; }
+    kp.xg = kp.ge; kp.xdrop = cfg->xdrop; kp.seed_len = cfg->seed_len;
+    kp.seed_count = cfg->seed_count; kp.flags = cfg->flags;
+    kp.ani_thr = cfg->ani_thr; kp.cov_thr = cfg->cov_thr;
+    kp.counter = (unsigned int *)base;
+    kp.status = (int *)(base + 16);
+    kp.exec_cells = (unsigned long long *)(base + 24);
+    kp.bnd = base + kNoAllocHeader;
+    kp.bnd_bytes = per_warp;
+    int nsm = 0, per_sm = 0;
+    CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, cfg->device));
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sw_noalloc<0>, pg::WARPS * 32, 0));
+    uint64_t grid = (uint64_t)nsm * (uint64_t)std::max(per_sm, 1);
+    grid = std::min<uint64_t>(grid, fit_warps / pg::WARPS);
+    grid = std::min<uint64_t>(grid, (n + pg::WARPS - 1) / pg::WARPS);
+    const dim3 blk(pg::WARPS * 32);
+    switch (cfg->tie) {
+    case 0: k_sw_noalloc<0><<<(unsigned)grid, blk, 0, st>>>(kp, (int)max_col_len); break;
+    case 1: k_sw_noalloc<1><<<(unsigned)grid, blk, 0, st>>>(kp, (int)max_col_len); break;
+    case 2: k_sw_noalloc<2><<<(unsigned)grid, blk, 0, st>>>(kp, (int)max_col_len); break;
+    default: k_sw_noalloc<3><<<(unsigned)grid, blk, 0, st>>>(kp, (int)max_col_len); break;
+    }
+    CU(cudaGetLastError());
+    int status = 0;
+    CU(cudaMemcpyAsync(&status, base + 16, sizeof status, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (status & pg::ST_BAD_INDEX)
+        return fail(PG_ERR_ARG, "pg_align_sw_noalloc: a pair refers to a sequence index out of range");
+    if (status & 2)
+        return fail(PG_ERR_RANGE, "pg_align_sw_noalloc: a column sequence is longer than max_col_len %u "
+                    "or a row sequence longer than 65535", max_col_len);
+    return PG_OK;
+}
