@@ -249,16 +249,24 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     CUD(cudaMalloc(&c->d_exec, sizeof(unsigned long long)));
     CUD(cudaMemset(c->d_exec, 0, sizeof(unsigned long long)));
     CUD(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, cfg->device));
+    CUD(cudaFuncSetAttribute(pg::k_ga<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_ga<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_ga<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_ga<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_sw<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_sw<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_sw<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_sw<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
     int per_sm = 0;
     if (cfg->mode == PG_MODE_XDROP) {
-        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pg::k_ga<0>, pg::WARPS * 32, 0));
+        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pg::k_ga<0>, pg::WARPS * 32, pg::DP_DYN_SMEM));
         int px = 0, pw = 0;
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&px, pg::k_xd, pg::XT, 0));
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pw, pg::k_xd_wide, pg::WARPS * 32, 0));
         c->grid_xd = c->nsm * std::max(px, 1);
         c->grid_wide = c->nsm * std::max(pw, 1);
     } else {
-        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pg::k_sw<0>, pg::WARPS * 32, 0));
+        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pg::k_sw<0>, pg::WARPS * 32, pg::DP_DYN_SMEM));
     }
     c->grid = c->nsm * std::max(per_sm, 1);
 #undef CUD
@@ -396,19 +404,21 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         const int gx = (int)std::min<uint64_t>((uint64_t)c->grid_xd, need_xd);
         pg::k_xd<<<gx, pg::XT, 0, st>>>(kp);
         pg::k_xd_wide<<<c->grid_wide, blk, 0, st>>>(kp);
+        const int dyn = pg::DP_DYN_SMEM;
         switch (c->cfg.tie) {
-        case 0: pg::k_ga<0><<<grid, blk, 0, st>>>(kp); break;
-        case 1: pg::k_ga<1><<<grid, blk, 0, st>>>(kp); break;
-        case 2: pg::k_ga<2><<<grid, blk, 0, st>>>(kp); break;
-        default: pg::k_ga<3><<<grid, blk, 0, st>>>(kp); break;
+        case 0: pg::k_ga<0><<<grid, blk, dyn, st>>>(kp); break;
+        case 1: pg::k_ga<1><<<grid, blk, dyn, st>>>(kp); break;
+        case 2: pg::k_ga<2><<<grid, blk, dyn, st>>>(kp); break;
+        default: pg::k_ga<3><<<grid, blk, dyn, st>>>(kp); break;
         }
         c->last_launches = 3;
     } else {
+        const int dyn = pg::DP_DYN_SMEM;
         switch (c->cfg.tie) {
-        case 0: pg::k_sw<0><<<grid, blk, 0, st>>>(kp); break;
-        case 1: pg::k_sw<1><<<grid, blk, 0, st>>>(kp); break;
-        case 2: pg::k_sw<2><<<grid, blk, 0, st>>>(kp); break;
-        default: pg::k_sw<3><<<grid, blk, 0, st>>>(kp); break;
+        case 0: pg::k_sw<0><<<grid, blk, dyn, st>>>(kp); break;
+        case 1: pg::k_sw<1><<<grid, blk, dyn, st>>>(kp); break;
+        case 2: pg::k_sw<2><<<grid, blk, dyn, st>>>(kp); break;
+        default: pg::k_sw<3><<<grid, blk, dyn, st>>>(kp); break;
         }
         c->last_launches = 1;
     }
@@ -569,6 +579,7 @@ __global__ void __launch_bounds__(pg::WARPS * 32) k_sw_noalloc(const pg::KParams
     const int lane = threadIdx.x & 31;
     const uint64_t gw = (uint64_t)blockIdx.x * pg::WARPS + (threadIdx.x >> 5);
     void *bnd = (char *)kp.bnd + gw * kp.bnd_bytes;
+    uint2 *prof = pg::g_dyn_prof + (threadIdx.x >> 5) * (pg::NCODES * 32);
     unsigned long long exec = 0;
     uint64_t p;
     while (pg::warp_fetch(&kp.counter[0], kp.n, p)) {
@@ -589,11 +600,11 @@ __global__ void __launch_bounds__(pg::WARPS * 32) k_sw_noalloc(const pg::KParams
         int score = 0, have = 0, ei = 0, ej = 0, i0 = 0, j0 = 0;
         uint32_t M = 0, D = 0, G = 0;
         if (m <= pg::L1::MAXSIDE && n <= pg::L1::MAXSIDE) {
-            const pg::DpOut<pg::L1> d = pg::dp_dispatch<pg::L1, TIE>(V, m, Hs, n, ssm, kp.go, kp.ge, bnd);
+            const pg::DpOut<pg::L1> d = pg::dp_dispatch<pg::L1, TIE>(V, m, Hs, n, ssm, prof, kp.go, kp.ge, bnd);
             score = d.score; have = d.have; ei = d.ei; ej = d.ej;
             M = d.st.M(); D = d.st.D(); G = d.st.G(); i0 = d.st.i0(); j0 = d.st.j0();
         } else {
-            const pg::DpOut<pg::L2> d = pg::dp_dispatch<pg::L2, TIE>(V, m, Hs, n, ssm, kp.go, kp.ge, bnd);
+            const pg::DpOut<pg::L2> d = pg::dp_dispatch<pg::L2, TIE>(V, m, Hs, n, ssm, prof, kp.go, kp.ge, bnd);
             score = d.score; have = d.have; ei = d.ei; ej = d.ej;
             M = d.st.M(); D = d.st.D(); G = d.st.G(); i0 = d.st.i0(); j0 = d.st.j0();
         }
@@ -657,6 +668,10 @@ extern "C" int pg_align_sw_noalloc(const pg_config *cfg,
             const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
             if (e != cudaSuccess || !ptr)
                 return fail(PG_ERR_CUDA, "pg_align_sw_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+            CU(cudaFuncSetAttribute(k_sw_noalloc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+            CU(cudaFuncSetAttribute(k_sw_noalloc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+            CU(cudaFuncSetAttribute(k_sw_noalloc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+            CU(cudaFuncSetAttribute(k_sw_noalloc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
             g_noalloc_ptr[cfg->device] = ptr;
         }
         base = (unsigned char *)g_noalloc_ptr[cfg->device];
@@ -687,16 +702,17 @@ extern "C" int pg_align_sw_noalloc(const pg_config *cfg,
     kp.bnd_bytes = per_warp;
     int nsm = 0, per_sm = 0;
     CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, cfg->device));
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sw_noalloc<0>, pg::WARPS * 32, 0));
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sw_noalloc<0>, pg::WARPS * 32, pg::DP_DYN_SMEM));
     uint64_t grid = (uint64_t)nsm * (uint64_t)std::max(per_sm, 1);
     grid = std::min<uint64_t>(grid, fit_warps / pg::WARPS);
     grid = std::min<uint64_t>(grid, (n + pg::WARPS - 1) / pg::WARPS);
     const dim3 blk(pg::WARPS * 32);
+    const int dyn = pg::DP_DYN_SMEM;
     switch (cfg->tie) {
-    case 0: k_sw_noalloc<0><<<(unsigned)grid, blk, 0, st>>>(kp, (int)max_col_len); break;
-    case 1: k_sw_noalloc<1><<<(unsigned)grid, blk, 0, st>>>(kp, (int)max_col_len); break;
-    case 2: k_sw_noalloc<2><<<(unsigned)grid, blk, 0, st>>>(kp, (int)max_col_len); break;
-    default: k_sw_noalloc<3><<<(unsigned)grid, blk, 0, st>>>(kp, (int)max_col_len); break;
+    case 0: k_sw_noalloc<0><<<(unsigned)grid, blk, dyn, st>>>(kp, (int)max_col_len); break;
+    case 1: k_sw_noalloc<1><<<(unsigned)grid, blk, dyn, st>>>(kp, (int)max_col_len); break;
+    case 2: k_sw_noalloc<2><<<(unsigned)grid, blk, dyn, st>>>(kp, (int)max_col_len); break;
+    default: k_sw_noalloc<3><<<(unsigned)grid, blk, dyn, st>>>(kp, (int)max_col_len); break;
     }
     CU(cudaGetLastError());
     int status = 0;

@@ -12,12 +12,21 @@
 //   E(i,j) = max(E(i,j-1) + ext, H(i,j-1) + first)      horizontal gap
 //   F(i,j) = max(F(i-1,j) + ext, H(i-1,j) + first)      vertical gap
 //   H(i,j) = max(H(i-1,j-1) + s, F, E [, 0])
-// The maxima use the DPX __vibmax_s32, whose predicate gives the winner.
-// Statistics (pg_stats.cuh) follow the predecessor a traceback would choose
-// under the tie policy TIE, so the end cell carries the statistics of the
-// traced alignment.  A gap opened from a cell whose best path already ends in
-// a gap of the same orientation continues that run (G unchanged), as in the
+// Inside a lane only F runs down the rows.  The lane carries A = F + ext and
+// G = H + first, so the chain from one row to the next is two DPX operations:
+//   F = vibmax(G_up, A_up)        G = viaddmax(F, first, max(diag, E) + first)
+// while the diagonal, E and every statistic select depend only on the previous
+// column and sit off that chain.  The DPX predicates give the winner of each
+// maximum; statistics (pg_stats.cuh) follow the predecessor a traceback would
+// choose under the tie policy TIE, so the end cell carries the statistics of
+// the traced alignment.  A gap opened from a cell whose best path already ends
+// in a gap of the same orientation continues that run (G unchanged), as in the
 // final alignment.
+//
+// Substitution scores come from a per-lane profile in shared memory: for each
+// residue code c, prof[c * 32 + lane] packs the scores of the lane's R rows
+// against c as int8 (rows 0-3 in .x, 4-7 in .y).  One 64-bit load per column
+// and lane, no bank conflicts, and a sign-extending byte extract per cell.
 #pragma once
 #include <cstdint>
 
@@ -27,6 +36,8 @@ namespace pg {
 
 constexpr int NEG = -(1 << 30);
 constexpr unsigned FULL = 0xffffffffu;
+constexpr int NCODES = 25;              // residue codes
+constexpr int PROF_BYTES = NCODES * 32 * 8;  // per-warp score profile
 
 constexpr int TIE_E_BEFORE_F = 1;
 constexpr int TIE_OPEN_FIRST = 2;
@@ -34,13 +45,13 @@ constexpr int TIE_OPEN_FIRST = 2;
 // values a lane hands down (the bottom row of its stripe at one column)
 template <class S>
 struct Edge {
-    int h, f;
+    int h, a;        // H, and F + ext
     S sf, shof, sh;  // F stats, stats for a vertical open from H, H stats
     __device__ __forceinline__ Edge shfl_up() const
     {
         Edge r;
         r.h = __shfl_up_sync(FULL, h, 1);
-        r.f = __shfl_up_sync(FULL, f, 1);
+        r.a = __shfl_up_sync(FULL, a, 1);
         r.sf = sf.shfl_up();
         r.shof = shof.shfl_up();
         r.sh = sh.shfl_up();
@@ -51,10 +62,10 @@ struct Edge {
 // Row 0 / column 0: the recurrence restricted to one direction.  Global: H =
 // first + (k-1) * max(first, ext), one gap run.  Local: 0, alignment restarts.
 template <class S>
-__device__ __forceinline__ Edge<S> border_row0(int j, int go, int gmax)
+__device__ __forceinline__ Edge<S> border_row0(int j, int go, int ge, int gmax)
 {
     Edge<S> e;
-    e.f = NEG;
+    e.a = NEG + ge;
     e.sf = S::zero();
     if (S::LOCAL) {
         e.h = 0;
@@ -73,22 +84,22 @@ __device__ __forceinline__ Edge<S> border_row0(int j, int go, int gmax)
 }
 
 template <class S>
-__device__ __forceinline__ Edge<S> border_col0(int i, int go, int gmax)
+__device__ __forceinline__ Edge<S> border_col0(int i, int go, int ge, int gmax)
 {
     Edge<S> e;
     if (S::LOCAL) {
-        e.h = 0; e.f = NEG;
+        e.h = 0; e.a = NEG + ge;
         e.sh = S::reset(i, 0);
         e.sf = S::zero();
         e.shof = e.sh.open();
     } else if (i == 0) {
-        e.h = 0; e.f = NEG;
+        e.h = 0; e.a = NEG + ge;
         e.sh = S::zero();
         e.sf = S::zero();
         e.shof = e.sh.open();
     } else {
         e.h = go + (i - 1) * gmax;
-        e.f = e.h;                   // column 0 is a vertical gap
+        e.a = e.h + ge;              // column 0 is a vertical gap: F = H
         e.sh = S::gap1();
         e.sf = e.sh;
         e.shof = e.sh;               // a further vertical gap continues the run
@@ -105,14 +116,16 @@ struct DpOut {
 };
 
 // Align V[0,m) (rows) with Hs[0,n) (columns).  ssm: 32x32 int score table in
-// shared memory indexed [v*32 + h].  bnd: per-warp scratch of n+1 edges (used
-// when m > 32*R).  All lanes return the same DpOut.
+// shared memory indexed [v*32 + h]; prof: this warp's profile buffer
+// (PROF_BYTES); bnd: per-warp scratch of n+1 edges (used when m > 32*R).  All
+// lanes return the same DpOut.
 template <class S, int TIE, int R>
 __device__ DpOut<S> dp_warp(const uint8_t *__restrict__ V, int m,
                             const uint8_t *__restrict__ Hs, int n,
-                            const int *__restrict__ ssm, int go, int ge,
-                            Edge<S> *__restrict__ bnd)
+                            const int *__restrict__ ssm, uint2 *__restrict__ prof,
+                            int go, int ge, Edge<S> *__restrict__ bnd)
 {
+    static_assert(R >= 1 && R <= 8, "profile holds up to 8 rows per lane");
     const int lane = threadIdx.x & 31;
     constexpr bool E_FIRST = (TIE & TIE_E_BEFORE_F) != 0;
     constexpr bool OPEN_FIRST = (TIE & TIE_OPEN_FIRST) != 0;
@@ -137,26 +150,47 @@ __device__ DpOut<S> dp_warp(const uint8_t *__restrict__ V, int m,
         const bool last_block = rb + rows_here >= m;
         const bool lane_on = lane <= t_last;
 
-        int vrow[R];
+        int vcode[R];
         bool valid[R];
-        int Hl[R], El[R];
+        int Hl[R], Gl[R], Al[R];
         S SHl[R], SEl[R], SHoEl[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int i = rb + lane * R + r + 1;
             valid[r] = lane_on && i <= m;
-            vrow[r] = valid[r] ? (int)__ldg(V + i - 1) * 32 : 0;
-            const Edge<S> c0 = border_col0<S>(i, go, gmax);
+            vcode[r] = valid[r] ? (int)__ldg(V + i - 1) : 255;
+            const Edge<S> c0 = border_col0<S>(i, go, ge, gmax);
             Hl[r] = c0.h;
-            El[r] = NEG;
+            Gl[r] = c0.h + go;
+            Al[r] = NEG + ge;          // no horizontal gap ends in column 0
             SHl[r] = c0.sh;
             SEl[r] = S::zero();
             SHoEl[r] = c0.sh.open();   // a horizontal gap from column 0 starts a run
         }
+        // this lane's score profile; lanes start at different residues so the
+        // table reads spread over banks
+        __syncwarp();
+        for (int q = 0; q < NCODES; ++q) {
+            int c = q + lane;
+            if (c >= NCODES) c -= NCODES;
+            if (c >= NCODES) c -= NCODES;
+            uint32_t lo = 0, hi = 0;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const uint32_t b = valid[r] ? ((uint32_t)ssm[vcode[r] * 32 + c] & 0xffu) : 0u;
+                if (r < 4) lo |= b << (8 * r);
+                else hi |= b << (8 * (r - 4));
+            }
+            prof[c * 32 + lane] = make_uint2(lo, hi);
+        }
+        __syncwarp();
+
         const int i_up = rb + lane * R;
         const int i_bot = min(rb + lane * R + R, m);
-        Edge<S> in = border_col0<S>(i_up, go, gmax);
-        Edge<S> out = border_col0<S>(i_bot, go, gmax);
+        Edge<S> in = border_col0<S>(i_up, go, ge, gmax);
+        Edge<S> out = border_col0<S>(i_bot, go, ge, gmax);
+        // residue of the column this lane works on next (prefetched one step ahead)
+        int hc_next = (lane == 0) ? (int)__ldg(Hs) : 0;
 
         const int nsteps = n + t_last;
         for (int k = 0; k < nsteps; ++k) {
@@ -165,70 +199,65 @@ __device__ DpOut<S> dp_warp(const uint8_t *__restrict__ V, int m,
             const S dgS = in.sh;
             if (lane == 0) {
                 const int jn = k + 1;
-                if (rb == 0) in = border_row0<S>(jn, go, gmax);
+                if (rb == 0) in = border_row0<S>(jn, go, ge, gmax);
                 else if (jn <= n) in = bnd[jn];
             } else {
                 in = rcv;
             }
             const int j = k - lane + 1;
+            const int hc = hc_next;
+            hc_next = (j >= 0 && j < n) ? (int)__ldg(Hs + j) : 0;
             if (lane_on && j >= 1 && j <= n) {
-                const int hc = (int)__ldg(Hs + j - 1);
-                int cH = in.h, cF = in.f;
+                const uint2 pw = prof[hc * 32 + lane];
+                int cG = in.h + go, cA = in.a, cH = in.h;
                 S cSF = in.sf, cSHoF = in.shof, cSH = in.sh;
                 int dH = dgH;
                 S dS = dgS;
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     if (!valid[r]) continue;
-                    const int s = ssm[vrow[r] + hc];
-                    // E (from the left)
+                    const int s = (int)(signed char)((r < 4 ? pw.x : pw.y) >> (8 * (r & 3)));
+                    // ---- off the row chain: E, diagonal, their maximum X
                     bool pe;
                     int E;
-                    if (OPEN_FIRST) { E = __vibmax_s32(Hl[r] + go, El[r] + ge, &pe); }
-                    else { bool px; E = __vibmax_s32(El[r] + ge, Hl[r] + go, &px); pe = !px; }
+                    if (OPEN_FIRST) { E = __vibmax_s32(Gl[r], Al[r], &pe); }
+                    else { bool px; E = __vibmax_s32(Al[r], Gl[r], &px); pe = !px; }
                     const S SE = S::sel(pe, SHoEl[r], SEl[r]);
-                    // F (from above)
+                    const int dg = dH + s;
+                    const S SD = dS.diag((uint32_t)(vcode[r] == hc));
+                    bool pX;                      // diagonal wins a tie with E
+                    int X = __vibmax_s32(dg, E, &pX);
+                    if (S::LOCAL) X = max(X, 0);
+                    const S SX = S::sel(pX, SD, SE);
+                    const S SXo = SX.open();
+                    // ---- the row chain
                     bool pf;
                     int F;
-                    if (OPEN_FIRST) { F = __vibmax_s32(cH + go, cF + ge, &pf); }
-                    else { bool px; F = __vibmax_s32(cF + ge, cH + go, &px); pf = !px; }
+                    if (OPEN_FIRST) { F = __vibmax_s32(cG, cA, &pf); }
+                    else { bool px; F = __vibmax_s32(cA, cG, &px); pf = !px; }
+                    const int G = __viaddmax_s32(F, go, X + go);
+                    const int A = F + ge;
+                    // ---- H and its statistics
+                    const int Hv = max(X, F);
+                    const bool chF = E_FIRST ? (F > X) : (F > dg && F >= E);
                     const S SF = S::sel(pf, cSHoF, cSF);
-                    // H
-                    const int dg = dH + s;
-                    const S SD = dS.diag((uint32_t)((vrow[r] >> 5) == hc));
-                    int Hv;
-                    bool chE, chF;
-                    S SH;
-                    if (E_FIRST) {
-                        bool p1, p2;
-                        const int t = __vibmax_s32(dg, E, &p1);
-                        Hv = __vibmax_s32(t, F, &p2);
-                        chF = !p2;
-                        chE = p2 && !p1;
-                        SH = S::sel(chF, SF, S::sel(chE, SE, SD));
-                    } else {
-                        bool p1, p2;
-                        const int t = __vibmax_s32(dg, F, &p1);
-                        Hv = __vibmax_s32(t, E, &p2);
-                        chE = !p2;
-                        chF = p2 && !p1;
-                        SH = S::sel(chE, SE, S::sel(chF, SF, SD));
-                    }
+                    S SH = S::sel(chF, SF, SX);
+                    S SHoF = S::sel(chF, SF, SXo);
+                    bool chE = !pX && !chF;
                     if (S::LOCAL) {
-                        if (Hv <= 0) {
-                            Hv = 0;
-                            chE = chF = false;
+                        if (Hv == 0) {
                             SH = S::reset(rb + lane * R + r + 1, j);
+                            SHoF = SH.open();
+                            chE = false;
                         }
                     }
-                    const S SHo = SH.open();
-                    const S SHoE = S::sel(chE, SH, SHo);
-                    const S SHoF = S::sel(chF, SH, SHo);
+                    const S SHoE = S::sel(chE, SH, SH.open());
                     // the old left value is the diagonal of the next row
                     dH = Hl[r];
                     dS = SHl[r];
-                    Hl[r] = Hv; El[r] = E; SEl[r] = SE; SHoEl[r] = SHoE; SHl[r] = SH;
-                    cH = Hv; cF = F; cSF = SF; cSHoF = SHoF; cSH = SH;
+                    Hl[r] = Hv; Gl[r] = G; Al[r] = E + ge;
+                    SEl[r] = SE; SHoEl[r] = SHoE; SHl[r] = SH;
+                    cG = G; cA = A; cH = Hv; cSF = SF; cSHoF = SHoF; cSH = SH;
                     if (S::LOCAL) {
                         // first maximum in column-major order; within a lane a
                         // later row block can only win a tie by a smaller column
@@ -237,7 +266,7 @@ __device__ DpOut<S> dp_warp(const uint8_t *__restrict__ V, int m,
                         }
                     }
                 }
-                out.h = cH; out.f = cF; out.sf = cSF; out.shof = cSHoF; out.sh = cSH;
+                out.h = cH; out.a = cA; out.sf = cSF; out.shof = cSHoF; out.sh = cSH;
                 if (!last_block && lane == t_last) bnd[j] = out;
             }
         }

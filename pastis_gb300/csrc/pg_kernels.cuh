@@ -260,14 +260,20 @@ __global__ void __launch_bounds__(WARPS * 32) k_xd_wide(const KParams kp)
 // lane, the wider ones stop at 4 to stay within the register budget
 template <class S, int TIE>
 __device__ __forceinline__ DpOut<S> dp_dispatch(const uint8_t *V, int m, const uint8_t *Hs, int n,
-                                                const int *ssm, int go, int ge, void *bnd)
+                                                const int *ssm, uint2 *prof, int go, int ge, void *bnd)
 {
     Edge<S> *b = (Edge<S> *)bnd;
     constexpr bool WIDE = sizeof(S) > 4;
-    if (m <= 64) return dp_warp<S, TIE, 2>(V, m, Hs, n, ssm, go, ge, b);
-    if (m <= 128 || WIDE) return dp_warp<S, TIE, 4>(V, m, Hs, n, ssm, go, ge, b);
-    return dp_warp<S, TIE, WIDE ? 4 : 8>(V, m, Hs, n, ssm, go, ge, b);
+    if (m <= 64) return dp_warp<S, TIE, 2>(V, m, Hs, n, ssm, prof, go, ge, b);
+    if (m <= 96) return dp_warp<S, TIE, 3>(V, m, Hs, n, ssm, prof, go, ge, b);
+    if (m <= 128 || WIDE) return dp_warp<S, TIE, 4>(V, m, Hs, n, ssm, prof, go, ge, b);
+    if (m <= 192) return dp_warp<S, TIE, WIDE ? 4 : 6>(V, m, Hs, n, ssm, prof, go, ge, b);
+    return dp_warp<S, TIE, WIDE ? 4 : 8>(V, m, Hs, n, ssm, prof, go, ge, b);
 }
+
+// dynamic shared memory of the warp-per-pair kernels: one score profile per warp
+constexpr int DP_DYN_SMEM = WARPS * PROF_BYTES;
+extern __shared__ uint2 g_dyn_prof[];
 
 template <int TIE>
 __global__ void __launch_bounds__(WARPS * 32, 2) k_ga(const KParams kp)
@@ -278,6 +284,7 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga(const KParams kp)
     const int lane = threadIdx.x & 31;
     const uint64_t gw = (uint64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
     void *bnd = (char *)kp.bnd + gw * kp.bnd_bytes;
+    uint2 *prof = g_dyn_prof + (threadIdx.x >> 5) * (NCODES * 32);
     unsigned long long exec = 0;
     uint64_t p;
     while (warp_fetch(&kp.counter[0], kp.n, p)) {
@@ -312,10 +319,10 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga(const KParams kp)
             int score;
             uint32_t M, D, G;
             if (rm <= S1::MAXSIDE && rn <= S1::MAXSIDE) {
-                const DpOut<S1> d = dp_dispatch<S1, TIE>(V + bv, rm, Hs + bh, rn, ssm, kp.go, kp.ge, bnd);
+                const DpOut<S1> d = dp_dispatch<S1, TIE>(V + bv, rm, Hs + bh, rn, ssm, prof, kp.go, kp.ge, bnd);
                 score = d.score; M = d.st.M(); D = d.st.D(); G = d.st.G();
             } else {
-                const DpOut<S2> d = dp_dispatch<S2, TIE>(V + bv, rm, Hs + bh, rn, ssm, kp.go, kp.ge, bnd);
+                const DpOut<S2> d = dp_dispatch<S2, TIE>(V + bv, rm, Hs + bh, rn, ssm, prof, kp.go, kp.ge, bnd);
                 score = d.score; M = d.st.M(); D = d.st.D(); G = d.st.G();
             }
             exec += area;
@@ -353,6 +360,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_sw(const KParams kp)
     const int lane = threadIdx.x & 31;
     const uint64_t gw = (uint64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
     void *bnd = (char *)kp.bnd + gw * kp.bnd_bytes;
+    uint2 *prof = g_dyn_prof + (threadIdx.x >> 5) * (NCODES * 32);
     unsigned long long exec = 0;
     uint64_t p;
     while (warp_fetch(&kp.counter[0], kp.n, p)) {
@@ -369,11 +377,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_sw(const KParams kp)
         int score = 0, have = 0, ei = 0, ej = 0, i0 = 0, j0 = 0;
         uint32_t M = 0, D = 0, G = 0;
         if (m <= L1::MAXSIDE && n <= L1::MAXSIDE) {
-            const DpOut<L1> d = dp_dispatch<L1, TIE>(V, m, Hs, n, ssm, kp.go, kp.ge, bnd);
+            const DpOut<L1> d = dp_dispatch<L1, TIE>(V, m, Hs, n, ssm, prof, kp.go, kp.ge, bnd);
             score = d.score; have = d.have; ei = d.ei; ej = d.ej;
             M = d.st.M(); D = d.st.D(); G = d.st.G(); i0 = d.st.i0(); j0 = d.st.j0();
         } else {
-            const DpOut<L2> d = dp_dispatch<L2, TIE>(V, m, Hs, n, ssm, kp.go, kp.ge, bnd);
+            const DpOut<L2> d = dp_dispatch<L2, TIE>(V, m, Hs, n, ssm, prof, kp.go, kp.ge, bnd);
             score = d.score; have = d.have; ei = d.ei; ej = d.ej;
             M = d.st.M(); D = d.st.D(); G = d.st.G(); i0 = d.st.i0(); j0 = d.st.j0();
         }
