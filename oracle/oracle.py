@@ -120,6 +120,16 @@ def global_(v, h, p):
     return out[0]
 
 
+def align_fast(v, h, p, local_):
+    """The packed DP the batch entry points use (must equal local()/global_())."""
+    v, h = _u8(v), _u8(h)
+    out = _res1()
+    lib().orc_align_fast(v.ctypes.data_as(ctypes.c_void_p), len(v), h.ctypes.data_as(ctypes.c_void_p),
+                         len(h), ctypes.byref(p), ctypes.c_int(1 if local_ else 0),
+                         out.ctypes.data_as(ctypes.c_void_p))
+    return out[0]
+
+
 def xdrop_extend(v, h, p, bh, eh, bv, ev):
     v, h = _u8(v), _u8(h)
     a = [ctypes.c_int(x) for x in (bh, eh, bv, ev)]

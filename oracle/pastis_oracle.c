@@ -213,6 +213,162 @@ static void dp_align(const uint8_t *v, int m, const uint8_t *h, int n,
     free(col);
 }
 
+/* The same DP with the per-row state in flat arrays and the statistics packed
+ * (md = M | D << 16, g = gap runs, b = i0 | j0 << 16), used by the batch entry
+ * points, which are also the timed CPU baseline.  Values and choices are those
+ * of dp_align (tests/test_oracle.py checks both on random pairs under every
+ * tie policy); only the bookkeeping differs. */
+typedef struct {
+    int *h, *e;
+    uint32_t *shm, *shg, *shb, *sem, *seg, *seb;
+    unsigned char *ch;
+    int cap;
+} fastbuf;
+
+static void fastbuf_reserve(fastbuf *fb, int rows)
+{
+    if (rows <= fb->cap) return;
+    free(fb->h); free(fb->e); free(fb->shm); free(fb->shg); free(fb->shb);
+    free(fb->sem); free(fb->seg); free(fb->seb); free(fb->ch);
+    fb->cap = rows + 64;
+    size_t k = (size_t)fb->cap;
+    fb->h = (int *)malloc(k * sizeof(int)); fb->e = (int *)malloc(k * sizeof(int));
+    fb->shm = (uint32_t *)malloc(k * 4); fb->shg = (uint32_t *)malloc(k * 4);
+    fb->shb = (uint32_t *)malloc(k * 4); fb->sem = (uint32_t *)malloc(k * 4);
+    fb->seg = (uint32_t *)malloc(k * 4); fb->seb = (uint32_t *)malloc(k * 4);
+    fb->ch = (unsigned char *)malloc(k);
+}
+
+static void fastbuf_free(fastbuf *fb)
+{
+    free(fb->h); free(fb->e); free(fb->shm); free(fb->shg); free(fb->shb);
+    free(fb->sem); free(fb->seg); free(fb->seb); free(fb->ch);
+    memset(fb, 0, sizeof *fb);
+}
+
+static void dp_align_fast(const uint8_t *v, int m, const uint8_t *hs, int n,
+                          const orc_params *p, int local, fastbuf *fb, orc_aln *out)
+{
+    const int go = p->gap_first, ge = p->gap_ext;
+    const int e_first = (p->tie & ORC_TIE_H_E_BEFORE_F) != 0;
+    const int open_first = (p->tie & ORC_TIE_GAP_OPEN_FIRST) != 0;
+    const int gmax = go > ge ? go : ge;
+    memset(out, 0, sizeof(*out));
+    if (m == 0 || n == 0) {
+        if (local) { out->flags = ORC_RF_EMPTY; return; }
+        if (m + n == 0) { out->flags = ORC_RF_EMPTY; return; }
+        out->score = go + (m + n - 1) * gmax;
+        out->aln_len = (uint32_t)(m + n); out->gap_opens = 1;
+        out->end_v = (uint16_t)m; out->end_h = (uint16_t)n;
+        out->identity = 0.0f;
+        return;
+    }
+    fastbuf_reserve(fb, m + 1);
+    int *H = fb->h, *E = fb->e;
+    uint32_t *SHm = fb->shm, *SHg = fb->shg, *SHb = fb->shb;
+    uint32_t *SEm = fb->sem, *SEg = fb->seg, *SEb = fb->seb;
+    unsigned char *CH = fb->ch;
+    /* column 0 */
+    for (int i = 0; i <= m; ++i) {
+        E[i] = NEG; SEm[i] = 0; SEg[i] = 0; SEb[i] = 0; SHm[i] = 0;
+        if (local) { H[i] = 0; CH[i] = CH_ZERO; SHg[i] = 0; SHb[i] = (uint32_t)i; }
+        else if (i == 0) { H[i] = 0; CH[i] = CH_DIAG; SHg[i] = 0; SHb[i] = 0; }
+        else { H[i] = go + (i - 1) * gmax; CH[i] = CH_F; SHg[i] = 1; SHb[i] = 0; }
+    }
+    int best = 0, bi = 0, bj = 0, have = 0;
+    uint32_t bm = 0, bg = 0, bb = 0;
+    for (int j = 1; j <= n; ++j) {
+        const int8_t *srow = p->sm + hs[j - 1];   /* column of the table: sm[v*25 + h] */
+        const uint8_t hj = hs[j - 1];
+        int dH = H[0];
+        uint32_t dm = SHm[0], dgg = SHg[0], db = SHb[0];
+        /* row 0 */
+        if (local) {
+            H[0] = 0; E[0] = NEG; CH[0] = CH_ZERO;
+            SHm[0] = 0; SHg[0] = 0; SHb[0] = (uint32_t)j << 16;
+        } else {
+            const int ext = E[0] + ge, opn = H[0] + go;
+            const int po = open_first ? (opn >= ext) : (opn > ext);
+            uint32_t sm_ = po ? SHm[0] : SEm[0];
+            uint32_t sg_ = po ? SHg[0] + (CH[0] != CH_E) : SEg[0];
+            E[0] = po ? opn : ext;
+            SEm[0] = sm_; SEg[0] = sg_; SEb[0] = 0;
+            H[0] = E[0]; SHm[0] = sm_; SHg[0] = sg_; SHb[0] = 0; CH[0] = CH_E;
+        }
+        int fU = NEG;                    /* F(i-1, j) */
+        uint32_t fm = 0, fg = 0, fb_ = 0;
+        for (int i = 1; i <= m; ++i) {
+            const uint8_t vi = v[i - 1];
+            /* E from the left (i, j-1) */
+            const int eext = E[i] + ge, eopn = H[i] + go;
+            const int pe = open_first ? (eopn >= eext) : (eopn > eext);
+            const int ev = pe ? eopn : eext;
+            const uint32_t em = pe ? SHm[i] : SEm[i];
+            const uint32_t eg = pe ? SHg[i] + (CH[i] != CH_E) : SEg[i];
+            const uint32_t eb = pe ? SHb[i] : SEb[i];
+            /* F from above (i-1, j): H[i-1] is already this column's */
+            const int fext = fU + ge, fopn = H[i - 1] + go;
+            const int pf = open_first ? (fopn >= fext) : (fopn > fext);
+            const int fv = pf ? fopn : fext;
+            const uint32_t nfm = pf ? SHm[i - 1] : fm;
+            const uint32_t nfg = pf ? SHg[i - 1] + (CH[i - 1] != CH_F) : fg;
+            const uint32_t nfb = pf ? SHb[i - 1] : fb_;
+            /* diagonal (i-1, j-1) */
+            const int dgv = dH + p->sm[vi * ORC_NRES + hj];
+            const uint32_t sdm = dm + (1u << 16) + (uint32_t)(vi == hj);
+            /* winner by priority, without branches: diag > F > E (or diag > E > F) */
+            int takeF, takeE;
+            if (e_first) {
+                const int me = ev > dgv;
+                takeF = fv > (me ? ev : dgv);
+                takeE = me && !takeF;
+            } else {
+                const int mf = fv > dgv;
+                takeE = ev > (mf ? fv : dgv);
+                takeF = mf && !takeE;
+            }
+            int hv = takeF ? fv : (takeE ? ev : dgv);
+            unsigned char ch = takeF ? CH_F : (takeE ? CH_E : CH_DIAG);
+            uint32_t hm = takeF ? nfm : (takeE ? em : sdm);
+            uint32_t hg = takeF ? nfg : (takeE ? eg : dgg);
+            uint32_t hb = takeF ? nfb : (takeE ? eb : db);
+            if (local) {
+                const int z = hv <= 0;
+                hv = z ? 0 : hv;
+                ch = z ? CH_ZERO : ch;
+                hm = z ? 0 : hm;
+                hg = z ? 0 : hg;
+                hb = z ? ((uint32_t)i | ((uint32_t)j << 16)) : hb;
+            }
+            dH = H[i]; dm = SHm[i]; dgg = SHg[i]; db = SHb[i];
+            H[i] = hv; E[i] = ev; CH[i] = ch;
+            SHm[i] = hm; SHg[i] = hg; SHb[i] = hb;
+            SEm[i] = em; SEg[i] = eg; SEb[i] = eb;
+            fU = fv; fm = nfm; fg = nfg; fb_ = nfb;
+            if (local && hv > best) { best = hv; bi = i; bj = j; bm = hm; bg = hg; bb = hb; have = 1; }
+        }
+        (void)srow;
+    }
+    uint32_t D, M, G;
+    int i0, j0, i1, j1;
+    if (local) {
+        if (!have) { out->flags = ORC_RF_EMPTY; return; }
+        out->score = best;
+        D = bm >> 16; M = bm & 0xffffu; G = bg;
+        i0 = (int)(bb & 0xffffu); j0 = (int)(bb >> 16); i1 = bi; j1 = bj;
+    } else {
+        out->score = H[m];
+        D = SHm[m] >> 16; M = SHm[m] & 0xffffu; G = SHg[m];
+        i0 = 0; j0 = 0; i1 = m; j1 = n;
+    }
+    uint32_t L = (uint32_t)((i1 - i0) + (j1 - j0)) - D;
+    out->aln_len = L; out->matches = M; out->gap_opens = G;
+    out->beg_v = (uint16_t)i0; out->end_v = (uint16_t)i1;
+    out->beg_h = (uint16_t)j0; out->end_h = (uint16_t)j1;
+    if (L == 0) { out->identity = 0.0f; out->flags |= ORC_RF_EMPTY; }
+    else out->identity = (float)((100.0 * (double)M) / (double)L);
+}
+
 void orc_local(const uint8_t *v, int m, const uint8_t *h, int n, const orc_params *p, orc_aln *out)
 {
     dp_align(v, m, h, n, p, 1, out);
@@ -373,11 +529,39 @@ void orc_sw_pair(const uint8_t *v, int m, const uint8_t *h, int n,
     apply_filter(out, m, n, p);
 }
 
+void orc_align_fast(const uint8_t *v, int m, const uint8_t *h, int n, const orc_params *p,
+                    int local, orc_aln *out)
+{
+    fastbuf fb; memset(&fb, 0, sizeof fb);
+    dp_align_fast(v, m, h, n, p, local, &fb, out);
+    fastbuf_free(&fb);
+    out->cells = sat32((uint64_t)m * (uint64_t)n);
+}
+
+static void sw_pair_fast(const uint8_t *v, int m, const uint8_t *h, int n,
+                         const orc_params *p, fastbuf *fb, orc_aln *out)
+{
+    dp_align_fast(v, m, h, n, p, 1, fb, out);
+    out->cells = sat32((uint64_t)m * (uint64_t)n);
+    out->seed_used = 0;
+    apply_filter(out, m, n, p);
+}
+
 /* src/align/SeqanXdropAligner.cpp:259-326: for each seed (first, second),
  * extend both ways, globally align the extended region, keep the strictly
  * higher identity; coverage uses the full sequence lengths (:340-341). */
+static void xdrop_pair_impl(const uint8_t *v, int m, const uint8_t *h, int n,
+                            const orc_pair *pr, const orc_params *p, fastbuf *fb, orc_aln *out);
+
 void orc_xdrop_pair(const uint8_t *v, int m, const uint8_t *h, int n,
                     const orc_pair *pr, const orc_params *p, orc_aln *out)
+{
+    xdrop_pair_impl(v, m, h, n, pr, p, NULL, out);
+}
+
+/* fb == NULL: the plain DP (dp_align); otherwise the packed one */
+static void xdrop_pair_impl(const uint8_t *v, int m, const uint8_t *h, int n,
+                            const orc_pair *pr, const orc_params *p, fastbuf *fb, orc_aln *out)
 {
     uint64_t cells = 0;
     int have = 0;
@@ -398,7 +582,8 @@ void orc_xdrop_pair(const uint8_t *v, int m, const uint8_t *h, int n,
         }
         cells += orc_xdrop_extend(v, m, h, n, p, &bh, &eh, &bv, &ev);
         orc_aln cur;
-        dp_align(v + bv, ev - bv, h + bh, eh - bh, p, 0, &cur);
+        if (fb) dp_align_fast(v + bv, ev - bv, h + bh, eh - bh, p, 0, fb, &cur);
+        else dp_align(v + bv, ev - bv, h + bh, eh - bh, p, 0, &cur);
         cells += (uint64_t)(ev - bv) * (uint64_t)(eh - bh);
         cur.beg_v = (uint16_t)bv; cur.end_v = (uint16_t)ev;
         cur.beg_h = (uint16_t)bh; cur.end_h = (uint16_t)eh;
@@ -436,17 +621,25 @@ int orc_batch(int mode,
         if (pairs[i].row + bl_roff >= nr || pairs[i].col + bl_coff >= nc) return -1;
 #ifdef _OPENMP
     if (nthreads <= 0) nthreads = omp_get_max_threads();
-#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+#pragma omp parallel num_threads(nthreads)
 #endif
-    for (long long i = 0; i < (long long)npairs; ++i) {
-        const orc_pair *pr = &pairs[i];
-        uint64_t r = pr->row + bl_roff, c = pr->col + bl_coff;
-        const uint8_t *v = rseq + roffs[r];
-        const uint8_t *h = cseq + coffs[c];
-        int m = (int)(roffs[r + 1] - roffs[r]);
-        int n = (int)(coffs[c + 1] - coffs[c]);
-        if (mode == 0) orc_sw_pair(v, m, h, n, p, &out[i]);
-        else orc_xdrop_pair(v, m, h, n, pr, p, &out[i]);
+    {
+        fastbuf fb;
+        memset(&fb, 0, sizeof fb);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 64)
+#endif
+        for (long long i = 0; i < (long long)npairs; ++i) {
+            const orc_pair *pr = &pairs[i];
+            uint64_t r = pr->row + bl_roff, c = pr->col + bl_coff;
+            const uint8_t *v = rseq + roffs[r];
+            const uint8_t *h = cseq + coffs[c];
+            int m = (int)(roffs[r + 1] - roffs[r]);
+            int n = (int)(coffs[c + 1] - coffs[c]);
+            if (mode == 0) sw_pair_fast(v, m, h, n, p, &fb, &out[i]);
+            else xdrop_pair_impl(v, m, h, n, pr, p, &fb, &out[i]);
+        }
+        fastbuf_free(&fb);
     }
     (void)nthreads;
     return 0;

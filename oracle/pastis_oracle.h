@@ -99,6 +99,11 @@ uint8_t orc_encode(char c);
 void orc_local(const uint8_t *v, int m, const uint8_t *h, int n, const orc_params *p, orc_aln *out);
 void orc_global(const uint8_t *v, int m, const uint8_t *h, int n, const orc_params *p, orc_aln *out);
 
+/* The same DP as orc_local / orc_global with packed bookkeeping (what the batch
+ * entry points use); local != 0 selects local alignment. */
+void orc_align_fast(const uint8_t *v, int m, const uint8_t *h, int n, const orc_params *p,
+                    int local, orc_aln *out);
+
 /* X-drop extension of one seed in both directions.  Seed = [*bh, *eh) x [*bv, *ev)
  * on entry and the extended region on exit.  Returns the number of band cells. */
 uint64_t orc_xdrop_extend(const uint8_t *v, int m, const uint8_t *h, int n,

@@ -213,9 +213,12 @@ __device__ DpOut<S> dp_warp(const uint8_t *__restrict__ V, int m,
                 S cSF = in.sf, cSHoF = in.shof, cSH = in.sh;
                 int dH = dgH;
                 S dS = dgS;
+                // Rows past m exist only at the end of the last lane's stripe:
+                // they are computed (no branch) but feed nothing downstream --
+                // the next lane is idle and the result is read from the last
+                // valid row -- and they never enter the local best.
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    if (!valid[r]) continue;
                     const int s = (int)(signed char)((r < 4 ? pw.x : pw.y) >> (8 * (r & 3)));
                     // ---- off the row chain: E, diagonal, their maximum X
                     bool pe;
@@ -261,7 +264,7 @@ __device__ DpOut<S> dp_warp(const uint8_t *__restrict__ V, int m,
                     if (S::LOCAL) {
                         // first maximum in column-major order; within a lane a
                         // later row block can only win a tie by a smaller column
-                        if (Hv > bs || (Hv == bs && Hv > 0 && j < bj)) {
+                        if (valid[r] && (Hv > bs || (Hv == bs && Hv > 0 && j < bj))) {
                             bs = Hv; bi = rb + lane * R + r + 1; bj = j; bst = SH;
                         }
                     }

@@ -152,52 +152,81 @@ __global__ void __launch_bounds__(XT) k_xd(const KParams kp)
     int *base = ring + threadIdx.x;
     const uint64_t ntask = 2 * kp.n;
     unsigned long long exec = 0;
+    // Each iteration a thread does one unit of its own extension: a cell, the
+    // close of an anti-diagonal, or the start of its next task.
+    XdState<XW, XT> st;
+    uint64_t task = 0;
+    const uint8_t *V = nullptr, *Hs = nullptr;
+    int m = 0, n = 0, bv = 0, ev = 0, bh = 0, eh = 0, dir = 0;
+    uint32_t flags = 0, cells = 0;
+    bool running = false;
     for (;;) {
-        const uint64_t task = atomicAdd(&kp.counter[1], 1u);
+        if (running) {
+            if (st.c < st.hi) {
+                st.cell(ssm, kp.xg, base);
+                continue;
+            }
+            if (st.close(base)) {
+                if (!st.open(kp.xg, kp.xdrop, base)) {
+                    // band outgrew the thread ring: k_xd_wide redoes this seed
+                    XdRec rec{0, 0, 0, 0, 0u, flags | XF_OVF};
+                    kp.xd[task] = rec;
+                    const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
+                    kp.ovf[slot] = (uint32_t)task;
+                    running = false;
+                }
+                continue;
+            }
+            int dv, dh;
+            st.finish(base, dv, dh);
+            cells += st.cells;
+            if (dir == 0) {
+                bv -= dv; bh -= dh;
+                if (ev < m && eh < n && st.start(V + ev, m - ev, 1, Hs + eh, n - eh, 1, kp.xg, kp.xdrop, base)) {
+                    dir = 1;
+                    st.open(kp.xg, kp.xdrop, base);
+                    continue;
+                }
+            } else {
+                ev += dv; eh += dh;
+            }
+            XdRec rec{(uint16_t)bv, (uint16_t)ev, (uint16_t)bh, (uint16_t)eh, cells, flags};
+            kp.xd[task] = rec;
+            exec += cells;
+            running = false;
+            continue;
+        }
+        task = atomicAdd(&kp.counter[1], 1u);
         if (task >= ntask) break;
         const uint64_t p = task >> 1;
         const int s = (int)(task & 1);
         const pg_pair pr = kp.pairs[p];
-        XdRec rec{0, 0, 0, 0, 0u, 0u};
-        const uint8_t *V, *Hs;
-        int m, n;
+        flags = 0; cells = 0;
         if (!pair_seqs(kp, pr, V, m, Hs, n)) {
-            rec.flags = XF_BADIDX;
-        } else if (s >= kp.seed_count ||
-                   (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
-            rec.flags = XF_NONE;
-        } else if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
-            rec.flags = XF_SAME;
-        } else {
-            int bv, ev, bh, eh;
-            if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
-            bool ok = true;
-            if (bv > 0 && bh > 0) {
-                const XdOut x = xdrop_dir_thread<XW, XT>(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1,
-                                                         ssm, kp.xg, kp.xdrop, base);
-                ok = x.ok;
-                rec.cells += x.cells;
-                bv -= x.dv; bh -= x.dh;
-            }
-            if (ok && ev < m && eh < n) {
-                const XdOut x = xdrop_dir_thread<XW, XT>(V + ev, m - ev, 1, Hs + eh, n - eh, 1,
-                                                         ssm, kp.xg, kp.xdrop, base);
-                ok = x.ok;
-                rec.cells += x.cells;
-                ev += x.dv; eh += x.dh;
-            }
-            if (ok) {
-                rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev;
-                rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
-                exec += rec.cells;
-            } else {
-                rec.flags |= XF_OVF;
-                rec.cells = 0;
-                const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
-                kp.ovf[slot] = (uint32_t)task;
-            }
+            kp.xd[task] = XdRec{0, 0, 0, 0, 0u, XF_BADIDX};
+            continue;
         }
-        kp.xd[task] = rec;
+        if (s >= kp.seed_count || (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
+            kp.xd[task] = XdRec{0, 0, 0, 0, 0u, XF_NONE};
+            continue;
+        }
+        if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
+            kp.xd[task] = XdRec{0, 0, 0, 0, 0u, XF_SAME};
+            continue;
+        }
+        if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) flags |= XF_BAD;
+        if (bv > 0 && bh > 0 &&
+            st.start(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1, kp.xg, kp.xdrop, base)) {
+            dir = 0;
+        } else if (ev < m && eh < n &&
+                   st.start(V + ev, m - ev, 1, Hs + eh, n - eh, 1, kp.xg, kp.xdrop, base)) {
+            dir = 1;
+        } else {
+            kp.xd[task] = XdRec{(uint16_t)bv, (uint16_t)ev, (uint16_t)bh, (uint16_t)eh, 0u, flags};
+            continue;
+        }
+        st.open(kp.xg, kp.xdrop, base);  // the first anti-diagonal always fits
+        running = true;
     }
     if (exec) atomicAdd(kp.exec_cells, exec);
 }

@@ -131,6 +131,116 @@ __device__ XdOut xdrop_dir_warp(const uint8_t *__restrict__ V, int nv, int vstep
     return o;
 }
 
+// One thread's extension as a resumable state machine.  xd_step() advances the
+// extension by one cell, or closes the current anti-diagonal (best, band
+// trimming, next anti-diagonal); a warp whose lanes run different extensions
+// thus computes cells together every iteration and diverges only for the
+// anti-diagonal bookkeeping.  The ring layout and every rule are those of
+// xdrop_dir_thread below.
+template <int W, int NT>
+struct XdState {
+    const uint8_t *V, *Hs;
+    int vstep, hstep, cols, rows;
+    int d, lo, hi, best, dbest, thr, c, a2prev;
+    int off1, len1, off2, len2, off3, len3;
+    int k1, k2, k3;
+    uint32_t cells;
+
+    __device__ __forceinline__ int &ring(int *base, int k, int col) const
+    {
+        return base[(k * W + (col & (W - 1))) * NT];
+    }
+
+    // start one direction; false if there is nothing to extend
+    __device__ __forceinline__ bool start(const uint8_t *v, int nv, int vs, const uint8_t *h, int nh, int hs,
+                                          int g, int X, int *base)
+    {
+        V = v; Hs = h; vstep = vs; hstep = hs; cols = nv + 1; rows = nh + 1;
+        cells = 0;
+        if (cols == 1 || rows == 1) return false;
+        k1 = 0; k2 = 1; k3 = 2;
+        off1 = 0; len1 = 0; off2 = 0; len2 = 1; off3 = 0; len3 = 2;
+        ring(base, k2, 0) = 0;
+        const int v1 = (-g > X) ? UND : g;
+        ring(base, k3, 0) = v1;
+        ring(base, k3, 1) = v1;
+        best = 0; d = 1; lo = 1; hi = 2;
+        return true;
+    }
+
+    // open anti-diagonal d+1 over [lo, hi); false on ring overflow
+    __device__ __forceinline__ bool open(int g, int X, int *base)
+    {
+        ++d;
+        const int kt = k1; k1 = k2; k2 = k3; k3 = kt;
+        off1 = off2; len1 = len2;
+        off2 = off3; len2 = len3;
+        off3 = lo - 1; len3 = hi + 1 - off3;
+        if (len3 > W) return false;
+        thr = best - X;
+        const int bval = (d * g > best - X) ? d * g : UND;
+        ring(base, k3, off3) = (off3 == 0) ? bval : UND;
+        ring(base, k3, hi) = (d == hi && hi < cols) ? bval : UND;
+        dbest = d * g;
+        c = lo;
+        a2prev = ring(base, k2, lo - 1);
+        return true;
+    }
+
+    // one cell of the open anti-diagonal (requires c < hi)
+    __device__ __forceinline__ void cell(const int *ssm, int g, int *base)
+    {
+        const int a2c = ring(base, k2, c);
+        int v = max(a2prev, a2c) + g;
+        const int vr = __ldg(V + vstep * (c - 1));
+        const int hr = __ldg(Hs + hstep * (d - c - 1));
+        v = max(v, ring(base, k1, c - 1) + ssm[vr * 32 + hr]);
+        const bool live = v >= thr;
+        ring(base, k3, c) = live ? v : UND;
+        if (live) dbest = max(dbest, v);
+        a2prev = a2c;
+        ++c;
+    }
+
+    // close the anti-diagonal; true if the band is still alive
+    __device__ __forceinline__ bool close(int *base)
+    {
+        if (dbest > best) best = dbest;
+        cells += (uint32_t)(hi - lo);
+        while (lo - off3 < len3 && ring(base, k3, lo) == UND && lo - off2 - 1 < len2 &&
+               ring(base, k2, lo - 1) == UND)
+            ++lo;
+        while (hi - off3 > 0 && ring(base, k3, hi - 1) == UND && ring(base, k2, hi - 1) == UND)
+            --hi;
+        ++hi;
+        if (lo < d + 2 - rows) lo = d + 2 - rows;
+        if (hi > cols) hi = cols;
+        return lo < hi;
+    }
+
+    // end point of the finished extension: (V consumed, H consumed)
+    __device__ __forceinline__ void finish(int *base, int &dv, int &dh) const
+    {
+        int lc = off3 + len3 - 2, lr = d - lc, ls = ring(base, k3, lc);
+        if (ls == UND) {
+            const int ca = off2 + len2 - 2;
+            if (ring(base, k2, ca) != UND) {
+                lc = ca; lr = d - 1 - lc; ls = ring(base, k2, ca);
+            } else if (len2 > 2 && ring(base, k2, ca - 1) != UND) {
+                lc = ca - 1; lr = d - 1 - lc; ls = ring(base, k2, ca - 1);
+            }
+        }
+        if (ls == UND) {
+            for (int k = 0; k < len1; ++k) {
+                const int val = ring(base, k1, off1 + k);
+                if (val > ls) { ls = val; lc = off1 + k; lr = d - 2 - lc; }
+            }
+        }
+        dv = 0; dh = 0;
+        if (ls != UND) { dv = lc; dh = lr; }
+    }
+};
+
 // The same extension run by one thread.  The ring holds W ints per
 // anti-diagonal; slot (array k, column c) sits at base[(k*W + (c & (W-1))) * NT]
 // where base = ring + threadIdx.x, so the 32 lanes of a warp always touch 32

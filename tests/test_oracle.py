@@ -94,6 +94,26 @@ def test_local_dominates_xdrop_region(oracle_mod):
         assert g <= loc
 
 
+@pytest.mark.parametrize("tie", [0, 1, 2, 3])
+@pytest.mark.parametrize("gaps", [(-11, -2), (-2, -11), (-5, -5)])
+def test_packed_dp_equals_plain(oracle_mod, tie, gaps):
+    """The batch path's packed DP makes exactly the plain DP's choices."""
+    O = oracle_mod
+    rng = np.random.default_rng(100 + tie)
+    p = O.make_params(gap_first=gaps[0], gap_ext=gaps[1], tie=tie)
+    letters = O.encode("ARNDCQEGHILKMFPSTWYVW")
+    for k in range(150):
+        a = letters[rng.integers(0, len(letters), rng.integers(0, 70))]
+        b = a.copy() if k % 3 == 0 else letters[rng.integers(0, len(letters), rng.integers(0, 70))]
+        if k % 3 == 0 and len(b):
+            b[rng.random(len(b)) < 0.3] = letters[rng.integers(0, 20)]
+            b = np.delete(b, rng.integers(0, len(b), min(3, len(b))))
+        for local_ in (True, False):
+            slow = (O.local if local_ else O.global_)(a, b, p)
+            fast = O.align_fast(a, b, p, local_)
+            assert slow.tobytes() == fast.tobytes(), (k, local_, slow, fast)
+
+
 def test_batch_matches_single(oracle_mod):
     """orc_batch (OpenMP) equals the single-pair functions, in both modes."""
     O = oracle_mod
