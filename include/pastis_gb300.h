@@ -61,6 +61,9 @@ extern "C" {
 #define PG_RF_EMPTY     1   /* no alignment columns (identity reported as 0) */
 #define PG_RF_BAD_SEED  2   /* a seed ran past a sequence end and was clamped */
 #define PG_RF_PASSED    4   /* coverage/ANI filter passed, score_aln = identity/100 */
+#define PG_RF_FILTERED  8   /* pruned by the learned pair filter, not aligned */
+
+#define PG_FILTER_FEATURES 16  /* k-mer overlap features per pair */
 
 #define PG_NRES 25          /* residue codes, order ARNDCQEGHILKMFPSTWYVBZX*J */
 
@@ -147,6 +150,44 @@ int pg_last_launches(const pg_ctx *ctx);
  * Differs from the sum of pg_result::cells where the kernel skips a second
  * seed whose extension or alignment repeats the first one's. */
 unsigned long long pg_exec_cells(pg_ctx *ctx);
+/* The same split as out[0] = X-drop band cells, out[1] = alignment DP cells. */
+int pg_exec_cells_split(pg_ctx *ctx, unsigned long long out[2]);
+
+/* Device time of the last pg_align / pg_align_device call, measured with CUDA
+ * events on its stream: out[0] = seed extension (X-drop kernels; 0 for SW),
+ * out[1] = alignment with statistics.  Waits for that batch to finish. */
+int pg_kernel_ms(pg_ctx *ctx, float out[2]);
+
+/* ---- learned candidate-pair filter
+ * A learned form of the k-mer prune of pw_aln_batch (count <= ckthr or
+ * score <= mosthr drops a pair, src/DistPWRunner.cpp:48-54): a 16-64-64-1 ReLU
+ * network over k-mer overlap features, BF16 weights on the tensor cores with
+ * FP32 accumulation, trained by the library's own kernels. */
+typedef struct pg_filter pg_filter;
+
+int  pg_filter_create(int device, uint64_t seed, pg_filter **out);
+void pg_filter_destroy(pg_filter *f);
+int  pg_filter_nparams(void);
+/* copy the FP32 parameters out (get != 0) or in (get == 0) */
+int  pg_filter_params(pg_filter *f, float *host, int get);
+/* PG_FILTER_FEATURES bf16 features per pair into d_features (n x 16);
+ * waits for the stream */
+int  pg_filter_features(pg_filter *f, pg_ctx *ctx, const pg_pair *d_pairs, uint64_t n,
+                        uint64_t bl_roffset, uint64_t bl_coffset, void *d_features, void *stream);
+/* logits (FP32) of n feature rows */
+int  pg_filter_predict(pg_filter *f, const void *d_features, uint64_t n, float *d_logits, void *stream);
+/* gradients of the mean weighted binary cross-entropy with logits; the host
+ * buffer receives pg_filter_nparams() gradients followed by the loss */
+int  pg_filter_gradients(pg_filter *f, const void *d_features, const float *d_labels,
+                         const float *d_weights, uint64_t n, float *host_grad_and_loss, void *stream);
+/* one Adam step (beta 0.9 / 0.999) on a mini-batch; *loss (optional) gets its loss */
+int  pg_filter_train_step(pg_filter *f, const void *d_features, const float *d_labels,
+                          const float *d_weights, uint64_t n, float lr, float *loss, void *stream);
+/* Align only the pairs whose logit is >= threshold; the others get an empty
+ * result flagged PG_RF_FILTERED (score_aln 0).  *kept receives the count. */
+int  pg_align_filtered(pg_ctx *ctx, pg_filter *f, float threshold, const pg_pair *d_pairs, uint64_t n,
+                       uint64_t bl_roffset, uint64_t bl_coffset, pg_result *d_out, void *stream,
+                       uint64_t *kept);
 
 /* Local alignment (--sfa semantics, cfg->mode must be PG_MODE_SW) for callers
  * that may not allocate device memory: code inside a stream capture, plugins

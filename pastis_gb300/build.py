@@ -21,7 +21,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 
 
 def _targets():
-    cu = [os.path.join(CSRC, f) for f in ("pg_api.cu",)]
+    cu = [os.path.join(CSRC, f) for f in ("pg_api.cu", "pg_filter.cu")]
     cu_deps = cu + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
     cu_deps += [os.path.join(INC, "pastis_gb300.h")]
     host_src = [os.path.join(CSRC, "host.cpp")]

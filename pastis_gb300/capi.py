@@ -19,7 +19,7 @@ MODE_SW, MODE_XDROP = 0, 1
 GAPS_AS_CALLED, GAPS_NOMINAL = 0, 1
 TIE_H_E_BEFORE_F, TIE_GAP_OPEN_FIRST = 1, 2
 F_SKIP_SPURIOUS_SEED = 1
-RF_EMPTY, RF_BAD_SEED, RF_PASSED = 1, 2, 4
+RF_EMPTY, RF_BAD_SEED, RF_PASSED, RF_FILTERED = 1, 2, 4, 8
 NRES = 25
 LETTERS = "ARNDCQEGHILKMFPSTWYVBZX*J"
 
@@ -42,8 +42,12 @@ assert KMERLOC_DTYPE.itemsize == 16 and KMERLIGHT_DTYPE.itemsize == 8
 EXPORTS = {
     "libpastis_gb300.so": ["pg_config_default", "pg_create", "pg_destroy", "pg_set_seqs",
                            "pg_share_row_seqs", "pg_align", "pg_align_device", "pg_sync",
-                           "pg_last_launches", "pg_exec_cells", "pg_dpx_peak", "pg_strerror", "pg_last_error",
-                           "pg_version", "pg_align_sw_noalloc"],
+                           "pg_last_launches", "pg_exec_cells", "pg_exec_cells_split",
+                           "pg_kernel_ms", "pg_dpx_peak", "pg_strerror", "pg_last_error",
+                           "pg_version", "pg_align_sw_noalloc", "pg_filter_create",
+                           "pg_filter_destroy", "pg_filter_nparams", "pg_filter_params",
+                           "pg_filter_features", "pg_filter_predict", "pg_filter_gradients",
+                           "pg_filter_train_step", "pg_align_filtered"],
     "libpastis_synth.so": ["pg_synth_generate", "pg_synth_free", "pg_synth_nseqs",
                            "pg_synth_nres", "pg_synth_npairs", "pg_synth_seq", "pg_synth_offs",
                            "pg_synth_family", "pg_synth_pairs", "pg_synth_homolog",
@@ -93,9 +97,22 @@ def _declare(name, lib):
         lib.pg_last_launches.argtypes = [vp]
         lib.pg_exec_cells.argtypes = [vp]
         lib.pg_exec_cells.restype = ctypes.c_ulonglong
+        lib.pg_exec_cells_split.argtypes = [vp, vp]
+        lib.pg_kernel_ms.argtypes = [vp, vp]
         lib.pg_dpx_peak.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
         lib.pg_align_sw_noalloc.argtypes = [ctypes.POINTER(Config), vp, vp, u64, vp, vp, u64,
                                             ctypes.c_uint32, vp, u64, u64, u64, vp, vp]
+        lib.pg_filter_create.argtypes = [i32, u64, ctypes.POINTER(vp)]
+        lib.pg_filter_destroy.argtypes = [vp]
+        lib.pg_filter_destroy.restype = None
+        lib.pg_filter_params.argtypes = [vp, vp, i32]
+        lib.pg_filter_features.argtypes = [vp, vp, vp, u64, u64, u64, vp, vp]
+        lib.pg_filter_predict.argtypes = [vp, vp, u64, vp, vp]
+        lib.pg_filter_gradients.argtypes = [vp, vp, vp, vp, u64, vp, vp]
+        lib.pg_filter_train_step.argtypes = [vp, vp, vp, vp, u64, ctypes.c_float,
+                                             ctypes.POINTER(ctypes.c_float), vp]
+        lib.pg_align_filtered.argtypes = [vp, vp, ctypes.c_float, vp, u64, u64, u64, vp, vp,
+                                          ctypes.POINTER(ctypes.c_uint64)]
         lib.pg_strerror.argtypes = [i32]
         lib.pg_strerror.restype = ctypes.c_char_p
         lib.pg_last_error.restype = ctypes.c_char_p
@@ -208,6 +225,18 @@ class Context:
 
     def exec_cells(self):
         return int(self.lib.pg_exec_cells(self.h))
+
+    def exec_cells_split(self):
+        """(X-drop band cells, alignment DP cells) computed since creation."""
+        v = (ctypes.c_ulonglong * 2)()
+        _check(self.lib.pg_exec_cells_split(self.h, v))
+        return int(v[0]), int(v[1])
+
+    def kernel_ms(self):
+        """(extension ms, alignment ms) of the last batch (CUDA events)."""
+        v = (ctypes.c_float * 2)()
+        _check(self.lib.pg_kernel_ms(self.h, v))
+        return float(v[0]), float(v[1])
 
 
 ALIGN_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,

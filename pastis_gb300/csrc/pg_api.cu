@@ -135,7 +135,9 @@ struct pg_ctx {
     pg_result *d_out = nullptr;
     uint64_t cap = 0;
     int last_launches = 0;
-    unsigned long long exec_total = 0;
+    // timing of the last batch: [0] start, [1] extension done, [2] alignment done
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    bool events_valid = false;
 };
 
 extern "C" {
@@ -197,6 +199,8 @@ void pg_destroy(pg_ctx *ctx)
     cudaFree(ctx->d_ovf);
     cudaFree(ctx->d_pairs);
     cudaFree(ctx->d_out);
+    for (int k = 0; k < 3; ++k)
+        if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -246,8 +250,9 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     CUD(cudaMemcpy(c->d_sm, c->sm, sizeof c->sm, cudaMemcpyHostToDevice));
     CUD(cudaMalloc(&c->d_counter, 4 * sizeof(unsigned int)));
     CUD(cudaMalloc(&c->d_status, sizeof(int)));
-    CUD(cudaMalloc(&c->d_exec, sizeof(unsigned long long)));
-    CUD(cudaMemset(c->d_exec, 0, sizeof(unsigned long long)));
+    CUD(cudaMalloc(&c->d_exec, 2 * sizeof(unsigned long long)));
+    CUD(cudaMemset(c->d_exec, 0, 2 * sizeof(unsigned long long)));
+    for (int k = 0; k < 3; ++k) CUD(cudaEventCreate(&c->ev[k]));
     CUD(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, cfg->device));
     CUD(cudaFuncSetAttribute(pg::k_ga<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
     CUD(cudaFuncSetAttribute(pg::k_ga<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
@@ -399,11 +404,13 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
     const uint64_t need_blocks = (n + pg::WARPS - 1) / pg::WARPS;
     const int grid = (int)std::min<uint64_t>((uint64_t)c->grid, need_blocks);
     const dim3 blk(pg::WARPS * 32);
+    CU(cudaEventRecord(c->ev[0], st));
     if (c->cfg.mode == PG_MODE_XDROP) {
         const uint64_t need_xd = (2 * n + pg::XT - 1) / pg::XT;
         const int gx = (int)std::min<uint64_t>((uint64_t)c->grid_xd, need_xd);
         pg::k_xd<<<gx, pg::XT, 0, st>>>(kp);
         pg::k_xd_wide<<<c->grid_wide, blk, 0, st>>>(kp);
+        CU(cudaEventRecord(c->ev[1], st));
         const int dyn = pg::DP_DYN_SMEM;
         switch (c->cfg.tie) {
         case 0: pg::k_ga<0><<<grid, blk, dyn, st>>>(kp); break;
@@ -413,6 +420,7 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         }
         c->last_launches = 3;
     } else {
+        CU(cudaEventRecord(c->ev[1], st));
         const int dyn = pg::DP_DYN_SMEM;
         switch (c->cfg.tie) {
         case 0: pg::k_sw<0><<<grid, blk, dyn, st>>>(kp); break;
@@ -422,6 +430,8 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         }
         c->last_launches = 1;
     }
+    CU(cudaEventRecord(c->ev[2], st));
+    c->events_valid = true;
     CU(cudaGetLastError());
     return PG_OK;
 }
@@ -473,6 +483,25 @@ int pg_align(pg_ctx *c, const pg_pair *pairs, uint64_t n, uint64_t roff, uint64_
 }
 
 int pg_last_launches(const pg_ctx *c) { return c ? c->last_launches : 0; }
+
+}  // extern "C"
+
+// internal (not exported): the resident sequences of a context, for the pair
+// filter in pg_filter.cu
+int pg_internal_seqs(const pg_ctx *c, const uint8_t **rseq, const uint64_t **roffs, uint64_t *nr,
+                     const uint8_t **cseq, const uint64_t **coffs, uint64_t *nc, int *device,
+                     void **stream, int *mode)
+{
+    if (!c || !c->side[0].seq || !c->side[1].seq) return fail(PG_ERR_STATE, "sequences not set");
+    *rseq = c->side[0].seq; *roffs = c->side[0].offs; *nr = c->side[0].n;
+    *cseq = c->side[1].seq; *coffs = c->side[1].offs; *nc = c->side[1].n;
+    *device = c->cfg.device; *stream = (void *)c->stream; *mode = c->cfg.mode;
+    return PG_OK;
+}
+
+int pg_internal_fail(int code, const char *msg) { return fail(code, "%s", msg); }
+
+extern "C" {
 
 }  // extern "C"
 
@@ -537,11 +566,29 @@ int pg_dpx_peak(int device, double *ops_per_s)
 // cells computed by the kernels since the context was created
 unsigned long long pg_exec_cells(pg_ctx *c)
 {
-    if (!c) return 0;
-    unsigned long long v = 0;
-    cudaSetDevice(c->cfg.device);
-    cudaMemcpy(&v, c->d_exec, sizeof v, cudaMemcpyDeviceToHost);
-    return v;
+    unsigned long long v[2] = {0, 0};
+    if (pg_exec_cells_split(c, v) != PG_OK) return 0;
+    return v[0] + v[1];
+}
+
+int pg_exec_cells_split(pg_ctx *c, unsigned long long out[2])
+{
+    if (!c || !out) return fail(PG_ERR_ARG, "null argument");
+    CU(cudaSetDevice(c->cfg.device));
+    CU(cudaMemcpy(out, c->d_exec, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    return PG_OK;
+}
+
+int pg_kernel_ms(pg_ctx *c, float out[2])
+{
+    if (!c || !out) return fail(PG_ERR_ARG, "null argument");
+    out[0] = out[1] = 0.0f;
+    if (!c->events_valid) return PG_OK;
+    CU(cudaSetDevice(c->cfg.device));
+    CU(cudaEventSynchronize(c->ev[2]));
+    CU(cudaEventElapsedTime(&out[0], c->ev[0], c->ev[1]));
+    CU(cudaEventElapsedTime(&out[1], c->ev[1], c->ev[2]));
+    return PG_OK;
 }
 
 }  // extern "C"
@@ -619,7 +666,7 @@ __global__ void __launch_bounds__(pg::WARPS * 32) k_sw_noalloc(const pg::KParams
         pg::apply_filter(o, m, n, kp.cov_thr, kp.ani_thr);
         if (lane == 0) kp.out[p] = o;
     }
-    if (lane == 0 && exec) atomicAdd(kp.exec_cells, exec);
+    if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
 }
 
 // restores the caller's current device on every return path

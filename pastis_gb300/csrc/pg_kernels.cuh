@@ -58,7 +58,7 @@ struct KParams {
     double cov_thr;
     unsigned int *counter;        // [0] k_ga / k_sw pairs, [1] k_xd tasks, [2] overflow count
     int *status;                  // error bits
-    unsigned long long *exec_cells; // cells actually computed (whole batch)
+    unsigned long long *exec_cells; // cells actually computed: [0] X-drop bands, [1] DP
     XdRec *xd;                    // 2 per pair
     uint32_t *ovf;                // overflowed (pair, seed) tasks
     void *bnd;                    // per-warp row scratch
@@ -146,89 +146,85 @@ __device__ __forceinline__ bool seed_region(const KParams &kp, const pg_pair &pr
 __global__ void __launch_bounds__(XT) k_xd(const KParams kp)
 {
     __shared__ int ssm[32 * 32];
-    __shared__ int ring[3 * XW * XT];
     load_sm(ssm, kp.sm);
     __syncthreads();
-    int *base = ring + threadIdx.x;
+    const int k = threadIdx.x & 15;
+    const unsigned hm = (threadIdx.x & 16) ? 0xffff0000u : 0x0000ffffu;
     const uint64_t ntask = 2 * kp.n;
     unsigned long long exec = 0;
-    // Each iteration a thread does one unit of its own extension: a cell, the
-    // close of an anti-diagonal, or the start of its next task.
-    XdState<XW, XT> st;
+    // Each half-warp takes the next (pair, seed), extends it left then right
+    // one anti-diagonal per iteration, and writes the extended region.
+    Xd16 st;
+    st.live = false;
     uint64_t task = 0;
     const uint8_t *V = nullptr, *Hs = nullptr;
     int m = 0, n = 0, bv = 0, ev = 0, bh = 0, eh = 0, dir = 0;
     uint32_t flags = 0, cells = 0;
-    bool running = false;
+    bool have = false, done = false;
     for (;;) {
-        if (running) {
-            if (st.c < st.hi) {
-                st.cell(ssm, kp.xg, base);
+        __syncwarp();
+        if (__ballot_sync(FULL, !done) == 0) break;
+        if (done) continue;
+        if (!have) {
+            unsigned int t = 0;
+            if (k == 0) t = atomicAdd(&kp.counter[1], 1u);
+            task = __shfl_sync(hm, t, 0, 16);
+            if (task >= ntask) { done = true; continue; }
+            const uint64_t p = task >> 1;
+            const int s = (int)(task & 1);
+            const pg_pair pr = kp.pairs[p];
+            flags = 0; cells = 0;
+            if (!pair_seqs(kp, pr, V, m, Hs, n)) {
+                if (k == 0) kp.xd[task] = XdRec{0, 0, 0, 0, 0u, XF_BADIDX};
                 continue;
             }
-            if (st.close(base)) {
-                if (!st.open(kp.xg, kp.xdrop, base)) {
-                    // band outgrew the thread ring: k_xd_wide redoes this seed
-                    XdRec rec{0, 0, 0, 0, 0u, flags | XF_OVF};
-                    kp.xd[task] = rec;
+            if (s >= kp.seed_count || (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
+                if (k == 0) kp.xd[task] = XdRec{0, 0, 0, 0, 0u, XF_NONE};
+                continue;
+            }
+            if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
+                if (k == 0) kp.xd[task] = XdRec{0, 0, 0, 0, 0u, XF_SAME};
+                continue;
+            }
+            if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) flags |= XF_BAD;
+            dir = 0;
+            if (bv > 0 && bh > 0) st.start(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1, kp.xg, kp.xdrop);
+            else st.live = false;
+            have = true;
+        }
+        if (st.live) {
+            if (!st.step(ssm, kp.xg, kp.xdrop)) {
+                // band outgrew 16 slots: k_xd_wide redoes this seed
+                if (k == 0) {
+                    kp.xd[task] = XdRec{0, 0, 0, 0, 0u, flags | XF_OVF};
                     const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
                     kp.ovf[slot] = (uint32_t)task;
-                    running = false;
                 }
+                have = false;
                 continue;
             }
+            if (st.live) continue;
             int dv, dh;
-            st.finish(base, dv, dh);
+            st.finish(dv, dh);
             cells += st.cells;
-            if (dir == 0) {
-                bv -= dv; bh -= dh;
-                if (ev < m && eh < n && st.start(V + ev, m - ev, 1, Hs + eh, n - eh, 1, kp.xg, kp.xdrop, base)) {
-                    dir = 1;
-                    st.open(kp.xg, kp.xdrop, base);
-                    continue;
-                }
-            } else {
-                ev += dv; eh += dh;
-            }
-            XdRec rec{(uint16_t)bv, (uint16_t)ev, (uint16_t)bh, (uint16_t)eh, cells, flags};
-            kp.xd[task] = rec;
-            exec += cells;
-            running = false;
-            continue;
+            if (dir == 0) { bv -= dv; bh -= dh; }
+            else { ev += dv; eh += dh; }
         }
-        task = atomicAdd(&kp.counter[1], 1u);
-        if (task >= ntask) break;
-        const uint64_t p = task >> 1;
-        const int s = (int)(task & 1);
-        const pg_pair pr = kp.pairs[p];
-        flags = 0; cells = 0;
-        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
-            kp.xd[task] = XdRec{0, 0, 0, 0, 0u, XF_BADIDX};
-            continue;
-        }
-        if (s >= kp.seed_count || (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
-            kp.xd[task] = XdRec{0, 0, 0, 0, 0u, XF_NONE};
-            continue;
-        }
-        if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
-            kp.xd[task] = XdRec{0, 0, 0, 0, 0u, XF_SAME};
-            continue;
-        }
-        if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) flags |= XF_BAD;
-        if (bv > 0 && bh > 0 &&
-            st.start(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1, kp.xg, kp.xdrop, base)) {
-            dir = 0;
-        } else if (ev < m && eh < n &&
-                   st.start(V + ev, m - ev, 1, Hs + eh, n - eh, 1, kp.xg, kp.xdrop, base)) {
+        // a direction is done (or had nothing to extend)
+        if (dir == 0) {
             dir = 1;
-        } else {
-            kp.xd[task] = XdRec{(uint16_t)bv, (uint16_t)ev, (uint16_t)bh, (uint16_t)eh, 0u, flags};
-            continue;
+            if (ev < m && eh < n) {
+                st.start(V + ev, m - ev, 1, Hs + eh, n - eh, 1, kp.xg, kp.xdrop);
+                continue;
+            }
         }
-        st.open(kp.xg, kp.xdrop, base);  // the first anti-diagonal always fits
-        running = true;
+        if (k == 0) {
+            kp.xd[task] = XdRec{(uint16_t)bv, (uint16_t)ev, (uint16_t)bh, (uint16_t)eh, cells, flags};
+            exec += cells;
+        }
+        have = false;
     }
-    if (exec) atomicAdd(kp.exec_cells, exec);
+    if (k == 0 && exec) atomicAdd(kp.exec_cells, exec);
 }
 
 // ------------------------------------------------------------- k_xd_wide
@@ -376,7 +372,7 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga(const KParams kp)
         apply_filter(best, m, n, kp.cov_thr, kp.ani_thr);
         if (lane == 0) kp.out[p] = best;
     }
-    if (lane == 0 && exec) atomicAdd(kp.exec_cells, exec);
+    if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
 }
 
 // ------------------------------------------------------------------ k_sw
@@ -425,7 +421,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_sw(const KParams kp)
         apply_filter(o, m, n, kp.cov_thr, kp.ani_thr);
         if (lane == 0) kp.out[p] = o;
     }
-    if (lane == 0 && exec) atomicAdd(kp.exec_cells, exec);
+    if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
 }
 
 }  // namespace pg
