@@ -384,7 +384,8 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
     c->last_launches = 0;
     if (n == 0) return PG_OK;
     if (!c->side[0].seq || !c->side[1].seq) return fail(PG_ERR_STATE, "sequences not set");
-    if (n > 0xffffffffull) return fail(PG_ERR_ARG, "batch of %llu pairs exceeds 2^32-1", (unsigned long long)n);
+    // work counters are 32-bit and run up to about n + chunk * warps
+    if (n > 0x7fffffffull) return fail(PG_ERR_ARG, "batch of %llu pairs exceeds 2^31-1", (unsigned long long)n);
     pg::KParams kp;
     kp.pairs = d_pairs; kp.n = n; kp.roff = roff; kp.coff = coff;
     kp.rseq = c->side[0].seq; kp.roffs = c->side[0].offs; kp.nr = c->side[0].n;
@@ -629,7 +630,8 @@ __global__ void __launch_bounds__(pg::WARPS * 32) k_sw_noalloc(const pg::KParams
     uint2 *prof = pg::g_dyn_prof + (threadIdx.x >> 5) * (pg::NCODES * 32);
     unsigned long long exec = 0;
     uint64_t p;
-    while (pg::warp_fetch(&kp.counter[0], kp.n, p)) {
+    pg::WarpQueue q;
+    while (q.pop(&kp.counter[0], kp.n, p)) {
         const pg_pair pr = kp.pairs[p];
         const uint8_t *V, *Hs;
         int m, n;

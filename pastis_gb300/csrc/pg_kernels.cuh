@@ -107,14 +107,26 @@ __device__ __forceinline__ pg_result empty_result()
     return o;
 }
 
-__device__ __forceinline__ bool warp_fetch(unsigned int *counter, uint64_t n, uint64_t &task)
-{
-    unsigned int t = 0;
-    if ((threadIdx.x & 31) == 0) t = atomicAdd(counter, 1u);
-    t = __shfl_sync(FULL, t, 0);
-    task = t;
-    return task < n;
-}
+// Work stealing: one atomic on the shared counter hands a warp FETCH_CHUNK
+// consecutive pairs (1: measured no faster with 4, and single pairs balance best).
+constexpr unsigned FETCH_CHUNK = 1;
+
+struct WarpQueue {
+    uint64_t next = 0, end = 0;
+    __device__ __forceinline__ bool pop(unsigned int *counter, uint64_t n, uint64_t &task)
+    {
+        if (next >= end) {
+            unsigned int t = 0;
+            if ((threadIdx.x & 31) == 0) t = atomicAdd(counter, FETCH_CHUNK);
+            t = __shfl_sync(FULL, t, 0);
+            next = t;
+            end = (uint64_t)t + FETCH_CHUNK < n ? (uint64_t)t + FETCH_CHUNK : n;
+        }
+        if (next >= n) return false;
+        task = next++;
+        return true;
+    }
+};
 
 // a pair's sequences; false on a bad index
 __device__ __forceinline__ bool pair_seqs(const KParams &kp, const pg_pair &pr,
@@ -146,85 +158,60 @@ __device__ __forceinline__ bool seed_region(const KParams &kp, const pg_pair &pr
 __global__ void __launch_bounds__(XT) k_xd(const KParams kp)
 {
     __shared__ int ssm[32 * 32];
+    __shared__ int ring[3 * XW * XT];
     load_sm(ssm, kp.sm);
     __syncthreads();
-    const int k = threadIdx.x & 15;
-    const unsigned hm = (threadIdx.x & 16) ? 0xffff0000u : 0x0000ffffu;
+    int *base = ring + threadIdx.x;
     const uint64_t ntask = 2 * kp.n;
     unsigned long long exec = 0;
-    // Each half-warp takes the next (pair, seed), extends it left then right
-    // one anti-diagonal per iteration, and writes the extended region.
-    Xd16 st;
-    st.live = false;
-    uint64_t task = 0;
-    const uint8_t *V = nullptr, *Hs = nullptr;
-    int m = 0, n = 0, bv = 0, ev = 0, bh = 0, eh = 0, dir = 0;
-    uint32_t flags = 0, cells = 0;
-    bool have = false, done = false;
     for (;;) {
-        __syncwarp();
-        if (__ballot_sync(FULL, !done) == 0) break;
-        if (done) continue;
-        if (!have) {
-            unsigned int t = 0;
-            if (k == 0) t = atomicAdd(&kp.counter[1], 1u);
-            task = __shfl_sync(hm, t, 0, 16);
-            if (task >= ntask) { done = true; continue; }
-            const uint64_t p = task >> 1;
-            const int s = (int)(task & 1);
-            const pg_pair pr = kp.pairs[p];
-            flags = 0; cells = 0;
-            if (!pair_seqs(kp, pr, V, m, Hs, n)) {
-                if (k == 0) kp.xd[task] = XdRec{0, 0, 0, 0, 0u, XF_BADIDX};
-                continue;
+        const uint64_t task = atomicAdd(&kp.counter[1], 1u);
+        if (task >= ntask) break;
+        const uint64_t p = task >> 1;
+        const int s = (int)(task & 1);
+        const pg_pair pr = kp.pairs[p];
+        XdRec rec{0, 0, 0, 0, 0u, 0u};
+        const uint8_t *V, *Hs;
+        int m, n;
+        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
+            rec.flags = XF_BADIDX;
+        } else if (s >= kp.seed_count ||
+                   (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
+            rec.flags = XF_NONE;
+        } else if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
+            rec.flags = XF_SAME;
+        } else {
+            int bv, ev, bh, eh;
+            if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
+            bool ok = true;
+            if (bv > 0 && bh > 0) {
+                const XdOut x = xdrop_dir_thread<XW, XT>(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1,
+                                                         ssm, kp.xg, kp.xdrop, base);
+                ok = x.ok;
+                rec.cells += x.cells;
+                bv -= x.dv; bh -= x.dh;
             }
-            if (s >= kp.seed_count || (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
-                if (k == 0) kp.xd[task] = XdRec{0, 0, 0, 0, 0u, XF_NONE};
-                continue;
+            if (ok && ev < m && eh < n) {
+                const XdOut x = xdrop_dir_thread<XW, XT>(V + ev, m - ev, 1, Hs + eh, n - eh, 1,
+                                                         ssm, kp.xg, kp.xdrop, base);
+                ok = x.ok;
+                rec.cells += x.cells;
+                ev += x.dv; eh += x.dh;
             }
-            if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
-                if (k == 0) kp.xd[task] = XdRec{0, 0, 0, 0, 0u, XF_SAME};
-                continue;
-            }
-            if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) flags |= XF_BAD;
-            dir = 0;
-            if (bv > 0 && bh > 0) st.start(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1, kp.xg, kp.xdrop);
-            else st.live = false;
-            have = true;
-        }
-        if (st.live) {
-            if (!st.step(ssm, kp.xg, kp.xdrop)) {
-                // band outgrew 16 slots: k_xd_wide redoes this seed
-                if (k == 0) {
-                    kp.xd[task] = XdRec{0, 0, 0, 0, 0u, flags | XF_OVF};
-                    const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
-                    kp.ovf[slot] = (uint32_t)task;
-                }
-                have = false;
-                continue;
-            }
-            if (st.live) continue;
-            int dv, dh;
-            st.finish(dv, dh);
-            cells += st.cells;
-            if (dir == 0) { bv -= dv; bh -= dh; }
-            else { ev += dv; eh += dh; }
-        }
-        // a direction is done (or had nothing to extend)
-        if (dir == 0) {
-            dir = 1;
-            if (ev < m && eh < n) {
-                st.start(V + ev, m - ev, 1, Hs + eh, n - eh, 1, kp.xg, kp.xdrop);
-                continue;
+            if (ok) {
+                rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev;
+                rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
+                exec += rec.cells;
+            } else {
+                rec.flags |= XF_OVF;
+                rec.cells = 0;
+                const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
+                kp.ovf[slot] = (uint32_t)task;
             }
         }
-        if (k == 0) {
-            kp.xd[task] = XdRec{(uint16_t)bv, (uint16_t)ev, (uint16_t)bh, (uint16_t)eh, cells, flags};
-            exec += cells;
-        }
-        have = false;
+        kp.xd[task] = rec;
     }
-    if (k == 0 && exec) atomicAdd(kp.exec_cells, exec);
+    if (exec) atomicAdd(kp.exec_cells, exec);
 }
 
 // ------------------------------------------------------------- k_xd_wide
@@ -312,7 +299,8 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga(const KParams kp)
     uint2 *prof = g_dyn_prof + (threadIdx.x >> 5) * (NCODES * 32);
     unsigned long long exec = 0;
     uint64_t p;
-    while (warp_fetch(&kp.counter[0], kp.n, p)) {
+    WarpQueue q;
+    while (q.pop(&kp.counter[0], kp.n, p)) {
         const pg_pair pr = kp.pairs[p];
         const uint8_t *V, *Hs;
         int m, n;
@@ -388,7 +376,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_sw(const KParams kp)
     uint2 *prof = g_dyn_prof + (threadIdx.x >> 5) * (NCODES * 32);
     unsigned long long exec = 0;
     uint64_t p;
-    while (warp_fetch(&kp.counter[0], kp.n, p)) {
+    WarpQueue q;
+    while (q.pop(&kp.counter[0], kp.n, p)) {
         const pg_pair pr = kp.pairs[p];
         const uint8_t *V, *Hs;
         int m, n;

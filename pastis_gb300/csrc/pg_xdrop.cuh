@@ -131,241 +131,6 @@ __device__ XdOut xdrop_dir_warp(const uint8_t *__restrict__ V, int nv, int vstep
     return o;
 }
 
-// ------------------------------------------------------------------------
-// The extension run by a half-warp: 16 lanes, lane k holds slot k of each live
-// anti-diagonal (column off + k, the same slots the ring versions use), the
-// last three anti-diagonals in registers.  A band whose slots (interior plus
-// the two border slots) exceed 16 reports overflow.  The 16 lanes of a half
-// call the member functions together; every shuffle and ballot is masked to
-// the half (hm), so the two halves of a warp may run different tasks.
-struct Xd16 {
-    const uint8_t *V, *Hs;
-    int vstep, hstep, cols, rows;
-    int d, lo, hi, best;
-    int off1, len1, off2, len2, off3, len3;
-    int a1, a2, a3;      // this lane's slot of anti-diagonals d-2, d-1, d
-    uint32_t cells;
-    unsigned hm;         // lane mask of this half-warp
-    bool live;           // extension in progress
-
-    __device__ __forceinline__ int hmax(int v) const
-    {
-#pragma unroll
-        for (int o = 8; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(hm, v, o, 16));
-        return v;
-    }
-    __device__ __forceinline__ int hmin(int v) const
-    {
-#pragma unroll
-        for (int o = 8; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(hm, v, o, 16));
-        return v;
-    }
-
-    // set up one direction (uniform arguments across the half-warp)
-    __device__ __forceinline__ void start(const uint8_t *v, int nv, int vs, const uint8_t *h, int nh, int hs,
-                                          int g, int X)
-    {
-        const int k = threadIdx.x & 15;
-        hm = (threadIdx.x & 16) ? 0xffff0000u : 0x0000ffffu;
-        V = v; Hs = h; vstep = vs; hstep = hs; cols = nv + 1; rows = nh + 1;
-        cells = 0;
-        live = !(cols == 1 || rows == 1);
-        off1 = 0; len1 = 0; off2 = 0; len2 = 1; off3 = 0; len3 = 2;
-        a1 = UND;
-        a2 = (k == 0) ? 0 : UND;
-        const int v1 = (-g > X) ? UND : g;
-        a3 = (k < 2) ? v1 : UND;
-        best = 0; d = 1; lo = 1; hi = 2;
-    }
-
-    // Compute the next anti-diagonal and trim the band.  Returns false on
-    // overflow (the half-warp's task must be redone with a wider ring).
-    __device__ __forceinline__ bool step(const int *ssm, int g, int X)
-    {
-        const int k = threadIdx.x & 15;
-        ++d;
-        a1 = a2; a2 = a3;
-        off1 = off2; len1 = len2;
-        off2 = off3; len2 = len3;
-        off3 = lo - 1; len3 = hi + 1 - off3;
-        if (len3 > 16) return false;
-        const int d32 = off3 - off2, d31 = off3 - off1;
-        // source slots outside 0..15 (only ever needed by non-interior lanes,
-        // whose values are discarded) wrap inside the half
-        const int v2a = __shfl_sync(hm, a2, k + d32 - 1, 16);   // column c-1 on d-1
-        const int v2b = __shfl_sync(hm, a2, k + d32, 16);       // column c   on d-1
-        const int v1 = __shfl_sync(hm, a1, k + d31 - 1, 16);    // column c-1 on d-2
-        const int c = off3 + k;
-        const bool interior = k >= 1 && k <= len3 - 2;
-        const int thr = best - X;
-        int val = UND, lbest = d * g;
-        if (interior) {
-            const int vr = __ldg(V + vstep * (c - 1));
-            const int hr = __ldg(Hs + hstep * (d - c - 1));
-            const int t = max(max(v2a, v2b) + g, v1 + ssm[vr * 32 + hr]);
-            if (t >= thr) { val = t; lbest = max(lbest, t); }
-        } else {
-            const int bval = (d * g > best - X) ? d * g : UND;
-            if (k == 0) val = (off3 == 0) ? bval : UND;
-            else if (k == len3 - 1) val = (d == hi && hi < cols) ? bval : UND;
-        }
-        a3 = val;
-        const int db = hmax(lbest);
-        if (db > best) best = db;
-        cells += (uint32_t)(hi - lo);
-        // leading columns whose cell and left predecessor are dead
-        const bool tl = k >= 1 && k < len3 && val == UND && k + d32 - 1 < len2 && v2a == UND;
-        const unsigned half = (threadIdx.x & 16) ? 16u : 0u;
-        const unsigned nl = ((__ballot_sync(hm, !tl) >> half) & 0xffffu) & 0xfffeu;  // lanes >= 1
-        lo = off3 + (nl ? __ffs(nl) - 1 : 16);
-        // trailing columns whose cell and upper predecessor are dead
-        const int kmax = hi - 1 - off3;
-        const bool th = k <= kmax && val == UND && v2b == UND;
-        const unsigned nh = ((__ballot_sync(hm, !th && k <= kmax) >> half) & 0xffffu);
-        hi = nh ? off3 + (31 - __clz(nh)) + 1 : off3;
-        ++hi;
-        if (lo < d + 2 - rows) lo = d + 2 - rows;
-        if (hi > cols) hi = cols;
-        live = lo < hi;
-        return true;
-    }
-
-    // end point of a finished extension: (V consumed, H consumed)
-    __device__ __forceinline__ void finish(int &dv, int &dh) const
-    {
-        const int k = threadIdx.x & 15;
-        int lc = off3 + len3 - 2, lr = d - lc;
-        int ls = __shfl_sync(hm, a3, len3 - 2, 16);
-        if (ls == UND) {
-            const int s2 = __shfl_sync(hm, a2, len2 - 2, 16);
-            const int s3 = __shfl_sync(hm, a2, len2 >= 3 ? len2 - 3 : 0, 16);
-            if (s2 != UND) {
-                lc = off2 + len2 - 2; lr = d - 1 - lc; ls = s2;
-            } else if (len2 > 2 && s3 != UND) {
-                lc = off2 + len2 - 3; lr = d - 1 - lc; ls = s3;
-            }
-        }
-        if (ls == UND) {
-            const int v = (k < len1) ? a1 : UND;
-            const int mv = hmax(v);
-            const int mk = hmin((v == mv && mv != UND) ? k : 16);
-            if (mv != UND) { ls = mv; lc = off1 + mk; lr = d - 2 - lc; }
-        }
-        dv = 0; dh = 0;
-        if (ls != UND) { dv = lc; dh = lr; }
-    }
-};
-
-// One thread's extension as a resumable state machine.  xd_step() advances the
-// extension by one cell, or closes the current anti-diagonal (best, band
-// trimming, next anti-diagonal); a warp whose lanes run different extensions
-// thus computes cells together every iteration and diverges only for the
-// anti-diagonal bookkeeping.  The ring layout and every rule are those of
-// xdrop_dir_thread below.
-template <int W, int NT>
-struct XdState {
-    const uint8_t *V, *Hs;
-    int vstep, hstep, cols, rows;
-    int d, lo, hi, best, dbest, thr, c, a2prev;
-    int off1, len1, off2, len2, off3, len3;
-    int k1, k2, k3;
-    uint32_t cells;
-
-    __device__ __forceinline__ int &ring(int *base, int k, int col) const
-    {
-        return base[(k * W + (col & (W - 1))) * NT];
-    }
-
-    // start one direction; false if there is nothing to extend
-    __device__ __forceinline__ bool start(const uint8_t *v, int nv, int vs, const uint8_t *h, int nh, int hs,
-                                          int g, int X, int *base)
-    {
-        V = v; Hs = h; vstep = vs; hstep = hs; cols = nv + 1; rows = nh + 1;
-        cells = 0;
-        if (cols == 1 || rows == 1) return false;
-        k1 = 0; k2 = 1; k3 = 2;
-        off1 = 0; len1 = 0; off2 = 0; len2 = 1; off3 = 0; len3 = 2;
-        ring(base, k2, 0) = 0;
-        const int v1 = (-g > X) ? UND : g;
-        ring(base, k3, 0) = v1;
-        ring(base, k3, 1) = v1;
-        best = 0; d = 1; lo = 1; hi = 2;
-        return true;
-    }
-
-    // open anti-diagonal d+1 over [lo, hi); false on ring overflow
-    __device__ __forceinline__ bool open(int g, int X, int *base)
-    {
-        ++d;
-        const int kt = k1; k1 = k2; k2 = k3; k3 = kt;
-        off1 = off2; len1 = len2;
-        off2 = off3; len2 = len3;
-        off3 = lo - 1; len3 = hi + 1 - off3;
-        if (len3 > W) return false;
-        thr = best - X;
-        const int bval = (d * g > best - X) ? d * g : UND;
-        ring(base, k3, off3) = (off3 == 0) ? bval : UND;
-        ring(base, k3, hi) = (d == hi && hi < cols) ? bval : UND;
-        dbest = d * g;
-        c = lo;
-        a2prev = ring(base, k2, lo - 1);
-        return true;
-    }
-
-    // one cell of the open anti-diagonal (requires c < hi)
-    __device__ __forceinline__ void cell(const int *ssm, int g, int *base)
-    {
-        const int a2c = ring(base, k2, c);
-        int v = max(a2prev, a2c) + g;
-        const int vr = __ldg(V + vstep * (c - 1));
-        const int hr = __ldg(Hs + hstep * (d - c - 1));
-        v = max(v, ring(base, k1, c - 1) + ssm[vr * 32 + hr]);
-        const bool live = v >= thr;
-        ring(base, k3, c) = live ? v : UND;
-        if (live) dbest = max(dbest, v);
-        a2prev = a2c;
-        ++c;
-    }
-
-    // close the anti-diagonal; true if the band is still alive
-    __device__ __forceinline__ bool close(int *base)
-    {
-        if (dbest > best) best = dbest;
-        cells += (uint32_t)(hi - lo);
-        while (lo - off3 < len3 && ring(base, k3, lo) == UND && lo - off2 - 1 < len2 &&
-               ring(base, k2, lo - 1) == UND)
-            ++lo;
-        while (hi - off3 > 0 && ring(base, k3, hi - 1) == UND && ring(base, k2, hi - 1) == UND)
-            --hi;
-        ++hi;
-        if (lo < d + 2 - rows) lo = d + 2 - rows;
-        if (hi > cols) hi = cols;
-        return lo < hi;
-    }
-
-    // end point of the finished extension: (V consumed, H consumed)
-    __device__ __forceinline__ void finish(int *base, int &dv, int &dh) const
-    {
-        int lc = off3 + len3 - 2, lr = d - lc, ls = ring(base, k3, lc);
-        if (ls == UND) {
-            const int ca = off2 + len2 - 2;
-            if (ring(base, k2, ca) != UND) {
-                lc = ca; lr = d - 1 - lc; ls = ring(base, k2, ca);
-            } else if (len2 > 2 && ring(base, k2, ca - 1) != UND) {
-                lc = ca - 1; lr = d - 1 - lc; ls = ring(base, k2, ca - 1);
-            }
-        }
-        if (ls == UND) {
-            for (int k = 0; k < len1; ++k) {
-                const int val = ring(base, k1, off1 + k);
-                if (val > ls) { ls = val; lc = off1 + k; lr = d - 2 - lc; }
-            }
-        }
-        dv = 0; dh = 0;
-        if (ls != UND) { dv = lc; dh = lr; }
-    }
-};
-
 // The same extension run by one thread.  The ring holds W ints per
 // anti-diagonal; slot (array k, column c) sits at base[(k*W + (c & (W-1))) * NT]
 // where base = ring + threadIdx.x, so the 32 lanes of a warp always touch 32

@@ -10,7 +10,8 @@ target, and the plain aligner remains the judge of what the filter drops.
 
 Label: S >= T(m, n) = ceil((ln(K m n) + ln(1/E)) / lambda), the smallest score
 whose Karlin-Altschul E-value m n K exp(-lambda S) is at most E = 1e-3, with
-the published gapped BLOSUM62 parameters lambda = 0.267, K = 0.041.
+the published gapped BLOSUM62 parameters lambda = 0.267, K = 0.041; S is the
+local score under gap open -11 / extend -2 taken by name.
 """
 import ctypes
 import math
@@ -85,8 +86,10 @@ class Filter:
 
 
 def sw_labels(w, device=0):
-    """Local SW score of every pair (this library's kernel) and the label."""
-    ctx = capi.Context(capi.config(capi.MODE_SW, device=device))
+    """Local SW score of every pair (this library's kernel, gap open -11 /
+    extend -2 by name, the model the Karlin-Altschul parameters above are
+    published for) and the label."""
+    ctx = capi.Context(capi.config(capi.MODE_SW, device=device, gap_semantics=capi.GAPS_NOMINAL))
     ctx.set_seqs(0, w.ascii, w.offs)
     ctx.share_row_seqs()
     res = ctx.align(w.pairs)
