@@ -43,6 +43,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="CPU work per baseline sample (seconds)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-filter", action="store_true",
+                    help="skip the learned-filter arm (tuned_filtered)")
+    ap.add_argument("--filter-train-frac", type=float, default=0.5,
+                    help="training batch size as a fraction of the timed batch")
     return ap.parse_args()
 
 
@@ -345,6 +349,9 @@ def run_gpu(args, rank, world, local_rank):
                                          "the pair record and the result per pair"}},
             "wall_s_timed": t_wall,
         }
+    if rank == 0 and not args.no_filter:
+        line["tuned_filtered"] = filtered_arm(args, w, ctx, dev, stream, flush, d_pairs, res,
+                                              ms_step)
     if not args.no_cpu_baseline and rank == 0:
         cores = host_cores()
         p = oracle_params(cfg)
@@ -359,6 +366,77 @@ def run_gpu(args, rank, world, local_rank):
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def filtered_arm(args, w, ctx, dev, stream, flush, d_pairs, plain_res, plain_ms):
+    """The learned pair filter in front of the same aligner on the same batch.
+
+    A filter is trained (this library's BF16 kernels) on a separate batch of
+    the same generator, labelled by the SW kernel; its threshold keeps 99.5 %
+    of the positive validation pairs.  Timed per step: features, network,
+    compaction, alignment of the kept pairs, scatter of the results.  Recall
+    is measured on the timed batch itself against SW labels of every pair."""
+    import torch
+    from pastis_gb300 import capi, synth
+    from pastis_gb300 import filter as F
+    n = len(w.pairs)
+    wt = synth.generate(args.workload, seed=20260101 + 7919,
+                        scale=args.scale * args.filter_train_frac)
+    f, thr, fm = F.fit(wt, dev, recall=0.995)
+    _, labels = F.sw_labels(w, dev)
+    torch.cuda.set_stream(stream)
+    d_out = torch.empty(n * capi.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{dev}")
+    kept = 0
+    for _ in range(max(args.warmup, 3)):
+        kept = f.align_filtered(ctx, thr, d_pairs.data_ptr(), n, d_out.data_ptr(),
+                                stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    got = np.frombuffer(d_out.cpu().numpy().tobytes(), dtype=capi.RESULT_DTYPE)
+    keep = (got["flags"] & capi.RF_FILTERED) == 0
+    same = got[keep].tobytes() == plain_res[keep].tobytes()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)
+        ev[k][0].record(stream)
+        f.align_filtered(ctx, thr, d_pairs.data_ptr(), n, d_out.data_ptr(), stream.cuda_stream)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    # the filter's own share: features + network over the whole batch
+    feats = torch.empty(n * 32, dtype=torch.uint8, device=f"cuda:{dev}")
+    logits = torch.empty(n, dtype=torch.float32, device=f"cuda:{dev}")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.fill_(1)
+    e0.record(stream)
+    f.features(ctx, d_pairs.data_ptr(), n, feats.data_ptr(), stream.cuda_stream)
+    f.predict(feats.data_ptr(), n, logits.data_ptr(), stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    pos = labels > 0.5
+    out = {
+        "alignments_per_s": n / (ms * 1e-3),
+        "ms_per_step": ms,
+        "vs_plain_alignments_per_s": plain_ms / ms,
+        "kept_pairs": int(kept), "kept_fraction": kept / n,
+        "recall": float(keep[pos].mean()) if pos.any() else None,
+        "precision": float(pos[keep].mean()) if keep.any() else None,
+        "positives": int(pos.sum()),
+        "kept_results_identical_to_plain": bool(same),
+        "filter_ms": e0.elapsed_time(e1),
+        "threshold_logit": thr,
+        "label": "SW score (BLOSUM62, open -11 / extend -2) >= ceil((ln(K m n) + ln 1000) / "
+                 "lambda), lambda 0.267, K 0.041",
+        "training": {"pairs": fm["pairs"], "positive_fraction": fm["positive_fraction"],
+                     "label_s": fm["label_seconds"], "train_s": fm["train_seconds"],
+                     "val_recall": fm["val"]["recall"], "test_recall": fm["test"]["recall"],
+                     "test_kept_fraction": fm["test"]["kept_fraction"],
+                     "kmer_rule_kept_at_same_recall": fm["kmer_rule_kept_at_same_recall"]},
+        "alignments_per_s_counts": "candidate pairs resolved per second (pruned pairs get "
+                                   "score_aln 0 and the filtered flag)",
+    }
+    f.close()
+    return out
 
 
 def main():

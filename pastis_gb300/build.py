@@ -18,28 +18,36 @@ BUILD = os.path.join(HERE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC]
+CUDA_UNITS = ("pg_api.cu", "pg_filter.cu")
 
 
-def _targets():
-    cu = [os.path.join(CSRC, f) for f in ("pg_api.cu", "pg_filter.cu")]
-    cu_deps = cu + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
-    cu_deps += [os.path.join(INC, "pastis_gb300.h")]
+def _steps():
+    """Build steps in dependency order; each step is a list of independent
+    jobs (output name, command without -o, dependencies) run in parallel."""
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
+    headers += [os.path.join(INC, "pastis_gb300.h")]
+    objs = []
+    compile_jobs = []
+    for u in CUDA_UNITS:
+        src = os.path.join(CSRC, u)
+        obj = u.replace(".cu", ".o")
+        objs.append(os.path.join(BUILD, obj))
+        compile_jobs.append((obj, [NVCC] + NVCC_FLAGS + ["-c", src], [src] + headers))
+    synth = os.path.join(CSRC, "synth.c")
+    compile_jobs.append(("libpastis_synth.so",
+                         ["gcc", "-O3", "-std=c99", "-fopenmp", "-fPIC", "-shared", "-I", INC,
+                          synth, "-lm"],
+                         [synth, os.path.join(INC, "pastis_gb300_synth.h")]))
+    link = [("libpastis_gb300.so", [NVCC] + ARCH + ["-shared"] + objs, objs)]
     host_src = [os.path.join(CSRC, "host.cpp")]
-    return [
-        ("libpastis_gb300.so",
-         [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-                          "-I", INC] + cu,
-         cu_deps),
-        ("libpastis_synth.so",
-         ["gcc", "-O3", "-std=c99", "-fopenmp", "-fPIC", "-shared", "-I", INC,
-          os.path.join(CSRC, "synth.c"), "-lm"],
-         [os.path.join(CSRC, "synth.c"), os.path.join(INC, "pastis_gb300_synth.h")]),
-        ("libpastis_host.so",
-         ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", INC] + host_src
-         + ["-L", BUILD, "-lpastis_gb300", "-Wl,-rpath,$ORIGIN"],
-         host_src + [os.path.join(INC, "pastis_gb300_pwalign.hpp"),
-                     os.path.join(INC, "pastis_gb300.h")]),
-    ]
+    host = [("libpastis_host.so",
+             ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", INC] + host_src
+             + ["-L", BUILD, "-lpastis_gb300", "-Wl,-rpath,$ORIGIN"],
+             host_src + [os.path.join(BUILD, "libpastis_gb300.so"),
+                         os.path.join(INC, "pastis_gb300_pwalign.hpp"),
+                         os.path.join(INC, "pastis_gb300.h")])]
+    return [compile_jobs, link, host]
 
 
 def _stale(out, deps):
@@ -51,17 +59,13 @@ def _stale(out, deps):
 
 def build(force=False, verbose=False):
     os.makedirs(BUILD, exist_ok=True)
-    targets = [t for t in _targets() if os.path.exists(t[2][0])]
-    # the host library links against the CUDA library: build that first
-    first = [t for t in targets if t[0] != "libpastis_host.so"]
-    later = [t for t in targets if t[0] == "libpastis_host.so"]
-    for group in (first, later):
+    for jobs in _steps():
         procs = []
-        for name, cmd, deps in group:
+        for name, cmd, deps in jobs:
             out = os.path.join(BUILD, name)
             if not force and not _stale(out, deps):
                 continue
-            tmp = out + ".tmp%d" % os.getpid()
+            tmp = out + ".tmp%d" % os.getpid() + os.path.splitext(name)[1]
             full = cmd[:1] + ["-o", tmp] + cmd[1:]
             if verbose:
                 print(" ".join(full), file=sys.stderr)

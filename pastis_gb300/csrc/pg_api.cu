@@ -118,7 +118,7 @@ struct pg_ctx {
     Side side[2];
     bool cols_share_rows = false;
     // scratch
-    unsigned int *d_counter = nullptr;  // 3 work counters
+    unsigned int *d_counter = nullptr;  // 4 work counters, then the bucket schedule words
     int *d_status = nullptr;
     unsigned long long *d_exec = nullptr;
     void *d_bnd = nullptr;              // per-warp DP row scratch
@@ -130,6 +130,8 @@ struct pg_ctx {
     pg::XdRec *d_xd = nullptr;          // 2 extension records per pair
     uint32_t *d_ovf = nullptr;          // overflowed extension tasks
     uint64_t xd_cap = 0;
+    uint32_t *d_order = nullptr;        // bucket order of the pairs
+    uint64_t order_cap = 0;
     // staging for the host-buffer entry point
     pg_pair *d_pairs = nullptr;
     pg_result *d_out = nullptr;
@@ -197,6 +199,7 @@ void pg_destroy(pg_ctx *ctx)
     cudaFree(ctx->d_gring);
     cudaFree(ctx->d_xd);
     cudaFree(ctx->d_ovf);
+    cudaFree(ctx->d_order);
     cudaFree(ctx->d_pairs);
     cudaFree(ctx->d_out);
     for (int k = 0; k < 3; ++k)
@@ -248,7 +251,7 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     CUD(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CUD(cudaMalloc(&c->d_sm, sizeof c->sm));
     CUD(cudaMemcpy(c->d_sm, c->sm, sizeof c->sm, cudaMemcpyHostToDevice));
-    CUD(cudaMalloc(&c->d_counter, 4 * sizeof(unsigned int)));
+    CUD(cudaMalloc(&c->d_counter, (4 + pg::SCHED_WORDS) * sizeof(unsigned int)));
     CUD(cudaMalloc(&c->d_status, sizeof(int)));
     CUD(cudaMalloc(&c->d_exec, 2 * sizeof(unsigned long long)));
     CUD(cudaMemset(c->d_exec, 0, 2 * sizeof(unsigned long long)));
@@ -319,6 +322,12 @@ static int ensure_scratch(pg_ctx *c)
 // per-pair X-drop scratch for a batch of n pairs
 static int ensure_batch(pg_ctx *c, uint64_t n)
 {
+    if (n > c->order_cap) {
+        cudaFree(c->d_order);
+        c->d_order = nullptr; c->order_cap = 0;
+        CU(cudaMalloc(&c->d_order, n * sizeof(uint32_t)));
+        c->order_cap = n;
+    }
     if (c->cfg.mode != PG_MODE_XDROP || n <= c->xd_cap) return PG_OK;
     cudaFree(c->d_xd); cudaFree(c->d_ovf);
     c->d_xd = nullptr; c->d_ovf = nullptr; c->xd_cap = 0;
@@ -400,17 +409,21 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
     kp.xd = c->d_xd; kp.ovf = c->d_ovf;
     kp.bnd = c->d_bnd; kp.bnd_bytes = c->bnd_bytes;
     kp.gring = c->d_gring; kp.gring_w = c->gring_w;
-    CU(cudaMemsetAsync(c->d_counter, 0, 4 * sizeof(unsigned int), st));
+    kp.sched = c->d_counter + 4; kp.order = c->d_order;
+    CU(cudaMemsetAsync(c->d_counter, 0, (4 + pg::SCHED_WORDS) * sizeof(unsigned int), st));
     CU(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
     const uint64_t need_blocks = (n + pg::WARPS - 1) / pg::WARPS;
     const int grid = (int)std::min<uint64_t>((uint64_t)c->grid, need_blocks);
     const dim3 blk(pg::WARPS * 32);
+    const int gsched = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (n + 255) / 256);
     CU(cudaEventRecord(c->ev[0], st));
     if (c->cfg.mode == PG_MODE_XDROP) {
         const uint64_t need_xd = (2 * n + pg::XT - 1) / pg::XT;
         const int gx = (int)std::min<uint64_t>((uint64_t)c->grid_xd, need_xd);
         pg::k_xd<<<gx, pg::XT, 0, st>>>(kp);
         pg::k_xd_wide<<<c->grid_wide, blk, 0, st>>>(kp);
+        pg::k_hist<true><<<gsched, 256, 0, st>>>(kp);
+        pg::k_bucket<true><<<gsched, 256, 0, st>>>(kp);
         CU(cudaEventRecord(c->ev[1], st));
         const int dyn = pg::DP_DYN_SMEM;
         switch (c->cfg.tie) {
@@ -419,8 +432,10 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         case 2: pg::k_ga<2><<<grid, blk, dyn, st>>>(kp); break;
         default: pg::k_ga<3><<<grid, blk, dyn, st>>>(kp); break;
         }
-        c->last_launches = 3;
+        c->last_launches = 5;
     } else {
+        pg::k_hist<false><<<gsched, 256, 0, st>>>(kp);
+        pg::k_bucket<false><<<gsched, 256, 0, st>>>(kp);
         CU(cudaEventRecord(c->ev[1], st));
         const int dyn = pg::DP_DYN_SMEM;
         switch (c->cfg.tie) {
@@ -429,7 +444,7 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         case 2: pg::k_sw<2><<<grid, blk, dyn, st>>>(kp); break;
         default: pg::k_sw<3><<<grid, blk, dyn, st>>>(kp); break;
         }
-        c->last_launches = 1;
+        c->last_launches = 3;
     }
     CU(cudaEventRecord(c->ev[2], st));
     c->events_valid = true;
@@ -442,6 +457,7 @@ static int check_status(pg_ctx *c)
     int st = 0;
     CU(cudaMemcpy(&st, c->d_status, sizeof st, cudaMemcpyDeviceToHost));
     if (st & pg::ST_BAD_INDEX) return fail(PG_ERR_ARG, "a pair refers to a sequence index out of range");
+    if (st & pg::ST_BAD_SCHED) return fail(PG_ERR_CUDA, "internal: inconsistent bucket schedule");
     return PG_OK;
 }
 

@@ -32,6 +32,7 @@ constexpr int XW = 16;            // per-thread ring slots in k_xd
 
 // status word bits (read back by the host after a batch)
 constexpr int ST_BAD_INDEX = 1;
+constexpr int ST_BAD_SCHED = 4;   // bucket order inconsistent (never expected)
 
 // extension of one (pair, seed)
 constexpr uint32_t XF_NONE = 1;    // seed not tried (seed_count / spurious switch)
@@ -65,6 +66,8 @@ struct KParams {
     uint64_t bnd_bytes;           // bytes per warp
     int *gring;                   // per-warp fallback ring, 3 * gring_w ints each
     int gring_w;
+    unsigned int *sched = nullptr;   // [0, NBUCKET) bucket sizes, [NBUCKET, 2*NBUCKET) cursors
+    const uint32_t *order = nullptr; // pair taken as the t-th task by k_ga / k_sw (null: t)
 };
 
 __device__ __forceinline__ void load_sm(int *ssm, const int8_t *sm)
@@ -268,19 +271,119 @@ __global__ void __launch_bounds__(WARPS * 32) k_xd_wide(const KParams kp)
 }
 
 // ------------------------------------------------------------------ k_ga
-// stripe height by region height; the one-word statistics go up to 8 rows per
-// lane, the wider ones stop at 4 to stay within the register budget
+// Rows per lane by region height.  A stripe of 32*R rows costs (n + last
+// busy lane) column steps of R cells whatever number of its lanes hold rows,
+// so the region takes the fewest stripes of at most 32*RMAX rows and spreads
+// its rows evenly over them (m = 300: two stripes of R = 5, not 256 + 44 rows
+// at R = 8).  One-word statistics go up to 8 rows per lane, the wider ones
+// stop at 4 to stay within the register budget.
+template <class S>
+__host__ __device__ constexpr int dp_rows_max() { return sizeof(S) > 4 ? 4 : 8; }
+
+template <class S>
+__host__ __device__ __forceinline__ int dp_rows_per_lane(int m)
+{
+    constexpr int RMAX = dp_rows_max<S>();
+    const int stripes = m > 0 ? (m + 32 * RMAX - 1) / (32 * RMAX) : 1;
+    const int r = (m + 32 * stripes - 1) / (32 * stripes);
+    return r < 1 ? 1 : r;
+}
+
 template <class S, int TIE>
 __device__ __forceinline__ DpOut<S> dp_dispatch(const uint8_t *V, int m, const uint8_t *Hs, int n,
                                                 const int *ssm, uint2 *prof, int go, int ge, void *bnd)
 {
     Edge<S> *b = (Edge<S> *)bnd;
-    constexpr bool WIDE = sizeof(S) > 4;
-    if (m <= 64) return dp_warp<S, TIE, 2>(V, m, Hs, n, ssm, prof, go, ge, b);
-    if (m <= 96) return dp_warp<S, TIE, 3>(V, m, Hs, n, ssm, prof, go, ge, b);
-    if (m <= 128 || WIDE) return dp_warp<S, TIE, 4>(V, m, Hs, n, ssm, prof, go, ge, b);
-    if (m <= 192) return dp_warp<S, TIE, WIDE ? 4 : 6>(V, m, Hs, n, ssm, prof, go, ge, b);
-    return dp_warp<S, TIE, WIDE ? 4 : 8>(V, m, Hs, n, ssm, prof, go, ge, b);
+    constexpr int RM = dp_rows_max<S>();
+    switch (dp_rows_per_lane<S>(m)) {
+    case 1: return dp_warp<S, TIE, 1>(V, m, Hs, n, ssm, prof, go, ge, b);
+    case 2: return dp_warp<S, TIE, 2>(V, m, Hs, n, ssm, prof, go, ge, b);
+    case 3: return dp_warp<S, TIE, 3>(V, m, Hs, n, ssm, prof, go, ge, b);
+    case 4: return dp_warp<S, TIE, 4>(V, m, Hs, n, ssm, prof, go, ge, b);
+    case 5: return dp_warp<S, TIE, (RM < 5 ? RM : 5)>(V, m, Hs, n, ssm, prof, go, ge, b);
+    case 6: return dp_warp<S, TIE, (RM < 6 ? RM : 6)>(V, m, Hs, n, ssm, prof, go, ge, b);
+    case 7: return dp_warp<S, TIE, (RM < 7 ? RM : 7)>(V, m, Hs, n, ssm, prof, go, ge, b);
+    default: return dp_warp<S, TIE, RM>(V, m, Hs, n, ssm, prof, go, ge, b);
+    }
+}
+
+// ------------------------------------------------------------- schedule
+// k_ga / k_sw take their pairs in bucket order, one bucket per DP
+// instantiation (statistics width x rows per lane), widest and tallest first.
+// The warps of an SM then run the same one or two inner loops at a time: all
+// instantiations together are larger than the instruction cache, and mixing
+// them measured 1.4x slower.  Costly pairs also start first, so cheap ones
+// fill the tail of the batch.
+constexpr int NBUCKET = 16;
+constexpr int SCHED_WORDS = 2 * NBUCKET;
+constexpr int BUCKET_NONE = 12;   // no DP work
+
+// bucket of the first seed's region (X-drop) or of the pair (SW)
+template <bool XDROP>
+__device__ __forceinline__ int pair_bucket(const KParams &kp, uint64_t p)
+{
+    int m, n;
+    if (XDROP) {
+        const XdRec r = kp.xd[2 * p];
+        if (r.flags & (XF_NONE | XF_BADIDX)) return BUCKET_NONE;
+        m = r.ev - r.bv;
+        n = r.eh - r.bh;
+        if (m <= 0 || n <= 0) return BUCKET_NONE;
+        if (m > S1::MAXSIDE || n > S1::MAXSIDE) return 4 - dp_rows_per_lane<S2>(m);   // 0..3
+        return 12 - dp_rows_per_lane<S1>(m);                                           // 4..11
+    }
+    const pg_pair pr = kp.pairs[p];
+    const uint8_t *V, *Hs;
+    if (!pair_seqs(kp, pr, V, m, Hs, n) || m == 0 || n == 0) return BUCKET_NONE;
+    if (m > L1::MAXSIDE || n > L1::MAXSIDE) return 4 - dp_rows_per_lane<L2>(m);        // 0..3
+    return 8 - dp_rows_per_lane<L1>(m);                                                // 4..7
+}
+
+// bucket sizes
+template <bool XDROP>
+__global__ void __launch_bounds__(256) k_hist(const KParams kp)
+{
+    __shared__ unsigned int h[NBUCKET];
+    if (threadIdx.x < NBUCKET) h[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < kp.n;
+         p += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&h[pair_bucket<XDROP>(kp, p)], 1u);
+    __syncthreads();
+    if (threadIdx.x < NBUCKET && h[threadIdx.x]) atomicAdd(&kp.sched[threadIdx.x], h[threadIdx.x]);
+}
+
+// order[]: pairs grouped by bucket (any order inside a bucket)
+template <bool XDROP>
+__global__ void __launch_bounds__(256) k_bucket(const KParams kp)
+{
+    __shared__ unsigned int start[NBUCKET], h[NBUCKET], base[NBUCKET];
+    if (threadIdx.x == 0) {
+        unsigned int acc = 0;
+        for (int b = 0; b < NBUCKET; ++b) { start[b] = acc; acc += kp.sched[b]; }
+    }
+    uint32_t *order = const_cast<uint32_t *>(kp.order);
+    for (uint64_t c0 = (uint64_t)blockIdx.x * blockDim.x; c0 < kp.n; c0 += (uint64_t)gridDim.x * blockDim.x) {
+        if (threadIdx.x < NBUCKET) h[threadIdx.x] = 0;
+        __syncthreads();
+        const uint64_t p = c0 + threadIdx.x;
+        int b = 0;
+        unsigned int rank = 0;
+        if (p < kp.n) {
+            b = pair_bucket<XDROP>(kp, p);
+            rank = atomicAdd(&h[b], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x < NBUCKET && h[threadIdx.x])
+            base[threadIdx.x] = start[threadIdx.x] + atomicAdd(&kp.sched[NBUCKET + threadIdx.x], h[threadIdx.x]);
+        __syncthreads();
+        if (p < kp.n) {
+            const uint64_t pos = (uint64_t)base[b] + rank;
+            if (pos < kp.n) order[pos] = (uint32_t)p;
+            else atomicOr(kp.status, ST_BAD_SCHED);
+        }
+        __syncthreads();
+    }
 }
 
 // dynamic shared memory of the warp-per-pair kernels: one score profile per warp
@@ -300,7 +403,10 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga(const KParams kp)
     unsigned long long exec = 0;
     uint64_t p;
     WarpQueue q;
-    while (q.pop(&kp.counter[0], kp.n, p)) {
+    uint64_t t;
+    while (q.pop(&kp.counter[0], kp.n, t)) {
+        p = kp.order ? (uint64_t)kp.order[t] : t;
+        if (p >= kp.n) { if (lane == 0) atomicOr(kp.status, ST_BAD_SCHED); continue; }
         const pg_pair pr = kp.pairs[p];
         const uint8_t *V, *Hs;
         int m, n;
@@ -377,7 +483,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_sw(const KParams kp)
     unsigned long long exec = 0;
     uint64_t p;
     WarpQueue q;
-    while (q.pop(&kp.counter[0], kp.n, p)) {
+    uint64_t t;
+    while (q.pop(&kp.counter[0], kp.n, t)) {
+        p = kp.order ? (uint64_t)kp.order[t] : t;
+        if (p >= kp.n) { if (lane == 0) atomicOr(kp.status, ST_BAD_SCHED); continue; }
         const pg_pair pr = kp.pairs[p];
         const uint8_t *V, *Hs;
         int m, n;

@@ -177,3 +177,40 @@ def train(w, feats_dev, labels, device=0, epochs=4, batch=8192, lr=3e-3, pos_wei
 
 def capi_features():
     return 16
+
+
+def workload_features(w, device=0, mode=None):
+    """Features of every pair of a workload, on the device (torch uint8 tensor
+    holding n x 16 BF16 values)."""
+    import torch
+    mode = capi.MODE_XDROP if mode is None else mode
+    ctx = capi.Context(capi.config(mode, device=device))
+    ctx.set_seqs(0, w.ascii, w.offs)
+    ctx.share_row_seqs()
+    n = len(w.pairs)
+    dev = torch.device("cuda", device)
+    d_pairs = torch.from_numpy(w.pairs.view(np.uint8).copy()).to(dev)
+    feats = torch.empty(n * capi_features() * 2, dtype=torch.uint8, device=dev)
+    probe = Filter(device, seed=1)
+    probe.features(ctx, d_pairs.data_ptr(), n, feats.data_ptr())
+    torch.cuda.synchronize(dev)
+    probe.close()
+    ctx.close()
+    return feats
+
+
+def fit(w, device=0, recall=0.995, epochs=4, log=None):
+    """Label a training workload with the SW kernel, compute its features and
+    train a filter on them.  Returns (filter, threshold, metrics)."""
+    import time
+    t0 = time.perf_counter()
+    _, labels = sw_labels(w, device)
+    t1 = time.perf_counter()
+    feats = workload_features(w, device)
+    f, thr, m = train(w, feats, labels, device=device, epochs=epochs, recall=recall, log=log)
+    t2 = time.perf_counter()
+    m["label_seconds"] = t1 - t0
+    m["train_seconds"] = t2 - t1
+    m["pairs"] = int(len(labels))
+    m["positive_fraction"] = float(labels.mean())
+    return f, thr, m

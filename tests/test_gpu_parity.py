@@ -43,7 +43,7 @@ def run_both(mode, w, cfg, O, pairs=None, roff=0, coff=0, share=True):
     else:
         ctx.set_seqs(1, ascii_, w.offs)
     got = ctx.align(pairs, roff, coff)
-    assert ctx.last_launches() == (3 if mode == capi.MODE_XDROP else 1)
+    assert ctx.last_launches() == (5 if mode == capi.MODE_XDROP else 3)
     codes = O.encode(bytes(ascii_))
     exp = O.batch(mode, codes, w.offs, codes, w.offs, pairs, oracle_params(O, cfg),
                   bl_roff=roff, bl_coff=coff)
