@@ -30,6 +30,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "GCUPS & alignments/s, batched SW/X-drop: GPU plain vs tuned+filtered vs CPU"
 DPX_OPS_PER_CELL = 4  # E, F, H add-max and the max with the third term, int32
+SW_WORKLOADS = ("sw100k", "filter5m")
 
 
 def parse():
@@ -38,11 +39,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="xdrop1m", choices=["xdrop1m", "sw100k", "uneven10m"])
+    ap.add_argument("--workload", default="xdrop1m",
+                    choices=["xdrop1m", "sw100k", "uneven10m", "filter5m"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="CPU work per baseline sample (seconds)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the autotuned arm (tuned)")
     ap.add_argument("--no-filter", action="store_true",
                     help="skip the learned-filter arm (tuned_filtered)")
     ap.add_argument("--filter-train-frac", type=float, default=0.5,
@@ -60,6 +64,9 @@ def workload_desc(name, n, scale):
                   "synthetic proteins (lognormal lengths median 250 clamp 30-1000)",
         "uneven10m": "seeded X-drop, %d pairs over %d proteins, lengths 80%% lognormal "
                      "median 300 + 20%% uniform 1000-5000",
+        "filter5m": "affine Smith-Waterman + stats + coverage/ANI filter, %d pairs over %d "
+                    "synthetic proteins (lognormal lengths median 250 clamp 30-1000, 30%% "
+                    "homologs)",
     }[name]
     from pastis_gb300 import synth
     p = synth.PRESETS[name]
@@ -153,7 +160,7 @@ def run_reference(args, rank):
         return
     O.build()
     w = synth.generate(args.workload, seed=20260101, scale=args.scale)
-    mode = capi.MODE_SW if args.workload == "sw100k" else capi.MODE_XDROP
+    mode = capi.MODE_SW if args.workload in SW_WORKLOADS else capi.MODE_XDROP
     cfg = capi.config(mode)
     p = oracle_params(cfg)
     cores = host_cores()
@@ -199,7 +206,7 @@ def run_gpu(args, rank, world, local_rank):
         dist.init_process_group("nccl")
     dev = local_rank
     torch.cuda.set_device(dev)
-    mode = capi.MODE_SW if args.workload == "sw100k" else capi.MODE_XDROP
+    mode = capi.MODE_SW if args.workload in SW_WORKLOADS else capi.MODE_XDROP
     # weak scaling: every rank aligns its own batch of the same shape
     w = synth.generate(args.workload, seed=20260101 + rank, scale=args.scale)
     n = len(w.pairs)
@@ -349,9 +356,12 @@ def run_gpu(args, rank, world, local_rank):
                                          "the pair record and the result per pair"}},
             "wall_s_timed": t_wall,
         }
+    if rank == 0 and not args.no_tune:
+        line["tuned"] = tuned_arm(args, w, ctx, mode, dev, stream, flush, d_pairs, res, ms_step)
     if rank == 0 and not args.no_filter:
         line["tuned_filtered"] = filtered_arm(args, w, ctx, dev, stream, flush, d_pairs, res,
                                               ms_step)
+        line["tuned_filtered"]["tuning"] = ctx.get_tuning().as_dict()
     if not args.no_cpu_baseline and rank == 0:
         cores = host_cores()
         p = oracle_params(cfg)
@@ -368,6 +378,42 @@ def run_gpu(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+def tuned_arm(args, w, ctx, mode, dev, stream, flush, d_pairs, plain_res, plain_ms):
+    """The autotuned launch shape (pastis_gb300/autotune.py) with CUDA-graph
+    replay, on the same batch; the search runs on a sample of the batch."""
+    import torch
+    from pastis_gb300 import autotune, capi
+    n = len(w.pairs)
+    ns = min(n, 250_000)
+    d_out = torch.empty(n * capi.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{dev}")
+
+    def run_sample():
+        ctx.align_device(d_pairs.data_ptr(), ns, d_out.data_ptr(), stream.cuda_stream)
+
+    key = autotune.signature(mode, w.pairs, w.lengths())
+    best, rep = autotune.tune(ctx, run_sample, key=key, device=dev, use_cache=False)
+    for _ in range(max(args.warmup, 3)):
+        ctx.align_device(d_pairs.data_ptr(), n, d_out.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    got = np.frombuffer(d_out.cpu().numpy().tobytes(), dtype=capi.RESULT_DTYPE)
+    same = got.tobytes() == plain_res.tobytes()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)
+        ev[k][0].record(stream)
+        ctx.align_device(d_pairs.data_ptr(), n, d_out.data_ptr(), stream.cuda_stream)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    return {"alignments_per_s": n / (ms * 1e-3), "ms_per_step": ms,
+            "vs_plain_alignments_per_s": plain_ms / ms, "tuning": best,
+            "results_identical_to_plain": bool(same),
+            "search": {"sample_pairs": ns, "candidates": rep.get("candidates"),
+                       "seconds": rep.get("search_s"), "best_sample_ms": rep.get("ms"),
+                       "default_sample_ms": rep.get("default_ms"), "key": key}}
+
+
 def filtered_arm(args, w, ctx, dev, stream, flush, d_pairs, plain_res, plain_ms):
     """The learned pair filter in front of the same aligner on the same batch.
 
@@ -382,7 +428,9 @@ def filtered_arm(args, w, ctx, dev, stream, flush, d_pairs, plain_res, plain_ms)
     n = len(w.pairs)
     wt = synth.generate(args.workload, seed=20260101 + 7919,
                         scale=args.scale * args.filter_train_frac)
-    f, thr, fm = F.fit(wt, dev, recall=0.995)
+    # the threshold keeps 99.7 % of the validation positives so that the
+    # recall measured on the (different) timed batch stays above 99.5 %
+    f, thr, fm = F.fit(wt, dev, recall=0.997)
     _, labels = F.sw_labels(w, dev)
     torch.cuda.set_stream(stream)
     d_out = torch.empty(n * capi.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{dev}")

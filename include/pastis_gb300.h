@@ -143,8 +143,29 @@ int pg_align_device(pg_ctx *ctx, const pg_pair *d_pairs, uint64_t n,
                     void *stream);
 int pg_sync(pg_ctx *ctx);
 
-/* Number of kernel launches made by the last pg_align / pg_align_device call. */
+/* Number of kernel launches made by the last pg_align / pg_align_device call
+ * (with graph replay: the kernels of the replayed graph). */
 int pg_last_launches(const pg_ctx *ctx);
+
+/* ---- launch tuning (no reference counterpart: SeqAn has no launch shape).
+ * Every setting changes only how the batch is scheduled on the GPU; results
+ * are identical under all of them.  pastis_gb300/autotune.py picks them by
+ * timing candidates on a sample of the caller's own batch. */
+typedef struct pg_tuning {
+    int32_t dp_blocks_per_sm;   /* k_ga / k_sw resident blocks per SM; 0 = occupancy limit */
+    int32_t xd_blocks_per_sm;   /* k_xd resident blocks per SM; 0 = occupancy limit        */
+    int32_t bucket_order;       /* 1: pairs in DP-bucket order, tallest first; 0: input order */
+    int32_t rows_max;           /* cap on DP rows per lane, 1..8 (wide statistics stop at 4) */
+    int32_t graph;              /* 1: pg_align / pg_align_device capture the batch's launches
+                                   into a CUDA graph once per batch shape (pairs and output
+                                   pointers, n, offsets, stream) and replay it after that */
+    int32_t reserved[3];
+} pg_tuning;                    /* 32 bytes */
+
+void pg_tuning_default(pg_tuning *t);
+int  pg_get_tuning(const pg_ctx *ctx, pg_tuning *out);
+/* PG_ERR_ARG on a value out of range. */
+int  pg_set_tuning(pg_ctx *ctx, const pg_tuning *t);
 
 /* DP cells the kernels actually computed since pg_create (synchronizing read).
  * Differs from the sum of pg_result::cells where the kernel skips a second

@@ -47,7 +47,8 @@ EXPORTS = {
                            "pg_version", "pg_align_sw_noalloc", "pg_filter_create",
                            "pg_filter_destroy", "pg_filter_nparams", "pg_filter_params",
                            "pg_filter_features", "pg_filter_predict", "pg_filter_gradients",
-                           "pg_filter_train_step", "pg_align_filtered"],
+                           "pg_filter_train_step", "pg_align_filtered", "pg_tuning_default",
+                           "pg_get_tuning", "pg_set_tuning"],
     "libpastis_synth.so": ["pg_synth_generate", "pg_synth_free", "pg_synth_nseqs",
                            "pg_synth_nres", "pg_synth_npairs", "pg_synth_seq", "pg_synth_offs",
                            "pg_synth_family", "pg_synth_pairs", "pg_synth_homolog",
@@ -66,7 +67,25 @@ class Config(ctypes.Structure):
                 ("reserved", ctypes.c_int32), ("score_matrix", ctypes.c_void_p)]
 
 
+class Tuning(ctypes.Structure):
+    """pg_tuning: launch shape of a context (results never depend on it)."""
+    _fields_ = [("dp_blocks_per_sm", ctypes.c_int32), ("xd_blocks_per_sm", ctypes.c_int32),
+                ("bucket_order", ctypes.c_int32), ("rows_max", ctypes.c_int32),
+                ("graph", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+
+    FIELDS = ("dp_blocks_per_sm", "xd_blocks_per_sm", "bucket_order", "rows_max", "graph")
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k in self.FIELDS}
+
+
 _libs = {}
+
+
+def default_tuning():
+    t = Tuning()
+    load().pg_tuning_default(ctypes.byref(t))
+    return t
 
 
 def load(name="libpastis_gb300.so"):
@@ -100,6 +119,10 @@ def _declare(name, lib):
         lib.pg_exec_cells_split.argtypes = [vp, vp]
         lib.pg_kernel_ms.argtypes = [vp, vp]
         lib.pg_dpx_peak.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
+        lib.pg_tuning_default.argtypes = [vp]
+        lib.pg_tuning_default.restype = None
+        lib.pg_get_tuning.argtypes = [vp, vp]
+        lib.pg_set_tuning.argtypes = [vp, vp]
         lib.pg_align_sw_noalloc.argtypes = [ctypes.POINTER(Config), vp, vp, u64, vp, vp, u64,
                                             ctypes.c_uint32, vp, u64, u64, u64, vp, vp]
         lib.pg_filter_create.argtypes = [i32, u64, ctypes.POINTER(vp)]
@@ -237,6 +260,20 @@ class Context:
         v = (ctypes.c_float * 2)()
         _check(self.lib.pg_kernel_ms(self.h, v))
         return float(v[0]), float(v[1])
+
+    def get_tuning(self):
+        t = Tuning()
+        _check(self.lib.pg_get_tuning(self.h, ctypes.byref(t)))
+        return t
+
+    def set_tuning(self, t=None, **fields):
+        """Set a Tuning, or change the named fields of the current one."""
+        if t is None:
+            t = self.get_tuning()
+        for k, v in fields.items():
+            setattr(t, k, int(v))
+        _check(self.lib.pg_set_tuning(self.h, ctypes.byref(t)))
+        return t
 
 
 ALIGN_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,

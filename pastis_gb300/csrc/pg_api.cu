@@ -140,6 +140,22 @@ struct pg_ctx {
     // timing of the last batch: [0] start, [1] extension done, [2] alignment done
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     bool events_valid = false;
+    // launch tuning and the captured graph of the last batch shape
+    pg_tuning tune{};
+    int dp_per_sm = 1, xd_per_sm = 1;   // occupancy limits
+    uint64_t epoch = 0;                 // bumped whenever a buffer a graph holds moves
+    cudaGraphExec_t gexec = nullptr;
+    struct GraphKey {
+        const void *pairs, *out;
+        uint64_t n, roff, coff, epoch;
+        cudaStream_t st;
+        bool operator==(const GraphKey &o) const
+        {
+            return pairs == o.pairs && out == o.out && n == o.n && roff == o.roff &&
+                   coff == o.coff && epoch == o.epoch && st == o.st;
+        }
+    } gkey{};
+    int graph_launches = 0;
 };
 
 extern "C" {
@@ -204,6 +220,7 @@ void pg_destroy(pg_ctx *ctx)
     cudaFree(ctx->d_out);
     for (int k = 0; k < 3; ++k)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -277,6 +294,9 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pg::k_sw<0>, pg::WARPS * 32, pg::DP_DYN_SMEM));
     }
     c->grid = c->nsm * std::max(per_sm, 1);
+    c->dp_per_sm = std::max(per_sm, 1);
+    c->xd_per_sm = c->grid_xd ? c->grid_xd / c->nsm : 1;
+    pg_tuning_default(&c->tune);
 #undef CUD
     *out = c;
     return PG_OK;
@@ -300,6 +320,7 @@ static int ensure_scratch(pg_ctx *c)
         cudaFree(c->d_bnd);
         c->d_bnd = nullptr;
         c->bnd_bytes = 0;
+        ++c->epoch;
         CU(cudaMalloc(&c->d_bnd, per_warp * warps));
         c->bnd_bytes = per_warp;
         c->bnd_warps = warps;
@@ -311,6 +332,7 @@ static int ensure_scratch(pg_ctx *c)
             cudaFree(c->d_gring);
             c->d_gring = nullptr;
             c->gring_w = 0;
+            ++c->epoch;
             CU(cudaMalloc(&c->d_gring, (size_t)3 * gw * sizeof(int) * wwarps));
             c->gring_w = gw;
             c->gring_warps = wwarps;
@@ -325,12 +347,14 @@ static int ensure_batch(pg_ctx *c, uint64_t n)
     if (n > c->order_cap) {
         cudaFree(c->d_order);
         c->d_order = nullptr; c->order_cap = 0;
+        ++c->epoch;
         CU(cudaMalloc(&c->d_order, n * sizeof(uint32_t)));
         c->order_cap = n;
     }
     if (c->cfg.mode != PG_MODE_XDROP || n <= c->xd_cap) return PG_OK;
     cudaFree(c->d_xd); cudaFree(c->d_ovf);
     c->d_xd = nullptr; c->d_ovf = nullptr; c->xd_cap = 0;
+    ++c->epoch;
     CU(cudaMalloc(&c->d_xd, 2 * n * sizeof(pg::XdRec)));
     CU(cudaMalloc(&c->d_ovf, 2 * n * sizeof(uint32_t)));
     c->xd_cap = n;
@@ -373,6 +397,7 @@ int pg_set_seqs(pg_ctx *c, int32_t side, const char *residues, const uint64_t *o
     }
     s.n = n;
     s.maxlen = maxlen;
+    ++c->epoch;
     return ensure_scratch(c);
 }
 
@@ -384,6 +409,7 @@ int pg_share_row_seqs(pg_ctx *c)
     if (!c->cols_share_rows) { cudaFree(c->side[1].seq); cudaFree(c->side[1].offs); }
     c->side[1] = c->side[0];
     c->cols_share_rows = true;
+    ++c->epoch;
     return ensure_scratch(c);
 }
 
@@ -409,21 +435,31 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
     kp.xd = c->d_xd; kp.ovf = c->d_ovf;
     kp.bnd = c->d_bnd; kp.bnd_bytes = c->bnd_bytes;
     kp.gring = c->d_gring; kp.gring_w = c->gring_w;
-    kp.sched = c->d_counter + 4; kp.order = c->d_order;
+    kp.sched = c->d_counter + 4;
+    kp.order = c->tune.bucket_order ? c->d_order : nullptr;
+    kp.rows_cap = c->tune.rows_max;
     CU(cudaMemsetAsync(c->d_counter, 0, (4 + pg::SCHED_WORDS) * sizeof(unsigned int), st));
     CU(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
     const uint64_t need_blocks = (n + pg::WARPS - 1) / pg::WARPS;
-    const int grid = (int)std::min<uint64_t>((uint64_t)c->grid, need_blocks);
+    uint64_t gmax = (uint64_t)c->grid;
+    if (c->tune.dp_blocks_per_sm > 0)
+        gmax = std::min<uint64_t>(gmax, (uint64_t)c->nsm * (uint64_t)c->tune.dp_blocks_per_sm);
+    const int grid = (int)std::min<uint64_t>(gmax, need_blocks);
     const dim3 blk(pg::WARPS * 32);
     const int gsched = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (n + 255) / 256);
     CU(cudaEventRecord(c->ev[0], st));
     if (c->cfg.mode == PG_MODE_XDROP) {
         const uint64_t need_xd = (2 * n + pg::XT - 1) / pg::XT;
-        const int gx = (int)std::min<uint64_t>((uint64_t)c->grid_xd, need_xd);
+        uint64_t xmax = (uint64_t)c->grid_xd;
+        if (c->tune.xd_blocks_per_sm > 0)
+            xmax = std::min<uint64_t>(xmax, (uint64_t)c->nsm * (uint64_t)c->tune.xd_blocks_per_sm);
+        const int gx = (int)std::min<uint64_t>(xmax, need_xd);
         pg::k_xd<<<gx, pg::XT, 0, st>>>(kp);
         pg::k_xd_wide<<<c->grid_wide, blk, 0, st>>>(kp);
-        pg::k_hist<true><<<gsched, 256, 0, st>>>(kp);
-        pg::k_bucket<true><<<gsched, 256, 0, st>>>(kp);
+        if (kp.order) {
+            pg::k_hist<true><<<gsched, 256, 0, st>>>(kp);
+            pg::k_bucket<true><<<gsched, 256, 0, st>>>(kp);
+        }
         CU(cudaEventRecord(c->ev[1], st));
         const int dyn = pg::DP_DYN_SMEM;
         switch (c->cfg.tie) {
@@ -432,10 +468,12 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         case 2: pg::k_ga<2><<<grid, blk, dyn, st>>>(kp); break;
         default: pg::k_ga<3><<<grid, blk, dyn, st>>>(kp); break;
         }
-        c->last_launches = 5;
+        c->last_launches = kp.order ? 5 : 3;
     } else {
-        pg::k_hist<false><<<gsched, 256, 0, st>>>(kp);
-        pg::k_bucket<false><<<gsched, 256, 0, st>>>(kp);
+        if (kp.order) {
+            pg::k_hist<false><<<gsched, 256, 0, st>>>(kp);
+            pg::k_bucket<false><<<gsched, 256, 0, st>>>(kp);
+        }
         CU(cudaEventRecord(c->ev[1], st));
         const int dyn = pg::DP_DYN_SMEM;
         switch (c->cfg.tie) {
@@ -444,11 +482,40 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         case 2: pg::k_sw<2><<<grid, blk, dyn, st>>>(kp); break;
         default: pg::k_sw<3><<<grid, blk, dyn, st>>>(kp); break;
         }
-        c->last_launches = 3;
+        c->last_launches = kp.order ? 3 : 1;
     }
     CU(cudaEventRecord(c->ev[2], st));
     c->events_valid = true;
     CU(cudaGetLastError());
+    return PG_OK;
+}
+
+// launch() directly, or through a CUDA graph captured once per batch shape
+static int enqueue(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, uint64_t coff,
+                   pg_result *d_out, cudaStream_t st)
+{
+    if (!c->tune.graph || n == 0) return launch(c, d_pairs, n, roff, coff, d_out, st);
+    if (!c->side[0].seq || !c->side[1].seq) return fail(PG_ERR_STATE, "sequences not set");
+    int rc = ensure_batch(c, n);       // every allocation happens outside the capture
+    if (rc) return rc;
+    const pg_ctx::GraphKey key{d_pairs, d_out, n, roff, coff, c->epoch, st};
+    if (!c->gexec || !(key == c->gkey)) {
+        if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+        CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        rc = launch(c, d_pairs, n, roff, coff, d_out, st);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+        if (e != cudaSuccess) return fail(PG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        const cudaError_t e2 = cudaGraphInstantiate(&c->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e2 != cudaSuccess) { c->gexec = nullptr; return fail(PG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e2)); }
+        c->gkey = key;
+        c->graph_launches = c->last_launches;
+    }
+    CU(cudaGraphLaunch(c->gexec, st));
+    c->last_launches = c->graph_launches;
+    c->events_valid = true;
     return PG_OK;
 }
 
@@ -467,7 +534,7 @@ int pg_align_device(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff
     if (!c || (n > 0 && (!d_pairs || !d_out))) return fail(PG_ERR_ARG, "pg_align_device: bad argument");
     CU(cudaSetDevice(c->cfg.device));
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-    return launch(c, d_pairs, n, roff, coff, d_out, st);
+    return enqueue(c, d_pairs, n, roff, coff, d_out, st);
 }
 
 int pg_sync(pg_ctx *c)
@@ -492,7 +559,7 @@ int pg_align(pg_ctx *c, const pg_pair *pairs, uint64_t n, uint64_t roff, uint64_
         c->cap = n;
     }
     CU(cudaMemcpyAsync(c->d_pairs, pairs, n * sizeof(pg_pair), cudaMemcpyHostToDevice, c->stream));
-    int rc = launch(c, c->d_pairs, n, roff, coff, c->d_out, c->stream);
+    int rc = enqueue(c, c->d_pairs, n, roff, coff, c->d_out, c->stream);
     if (rc) return rc;
     CU(cudaMemcpyAsync(out, c->d_out, n * sizeof(pg_result), cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
@@ -500,6 +567,40 @@ int pg_align(pg_ctx *c, const pg_pair *pairs, uint64_t n, uint64_t roff, uint64_
 }
 
 int pg_last_launches(const pg_ctx *c) { return c ? c->last_launches : 0; }
+
+void pg_tuning_default(pg_tuning *t)
+{
+    if (!t) return;
+    std::memset(t, 0, sizeof *t);
+    t->dp_blocks_per_sm = 0;
+    t->xd_blocks_per_sm = 0;
+    t->bucket_order = 1;
+    t->rows_max = 8;
+    t->graph = 0;
+}
+
+int pg_get_tuning(const pg_ctx *c, pg_tuning *out)
+{
+    if (!c || !out) return fail(PG_ERR_ARG, "pg_get_tuning: bad argument");
+    *out = c->tune;
+    return PG_OK;
+}
+
+int pg_set_tuning(pg_ctx *c, const pg_tuning *t)
+{
+    if (!c || !t) return fail(PG_ERR_ARG, "pg_set_tuning: bad argument");
+    if (t->dp_blocks_per_sm < 0 || t->dp_blocks_per_sm > c->dp_per_sm)
+        return fail(PG_ERR_ARG, "dp_blocks_per_sm %d outside 0..%d", t->dp_blocks_per_sm, c->dp_per_sm);
+    if (t->xd_blocks_per_sm < 0 || t->xd_blocks_per_sm > 64)
+        return fail(PG_ERR_ARG, "xd_blocks_per_sm %d outside 0..64", t->xd_blocks_per_sm);
+    if (t->bucket_order != 0 && t->bucket_order != 1) return fail(PG_ERR_ARG, "bucket_order must be 0 or 1");
+    if (t->rows_max < 1 || t->rows_max > 8) return fail(PG_ERR_ARG, "rows_max %d outside 1..8", t->rows_max);
+    if (t->graph != 0 && t->graph != 1) return fail(PG_ERR_ARG, "graph must be 0 or 1");
+    c->tune = *t;
+    std::memset(c->tune.reserved, 0, sizeof c->tune.reserved);
+    ++c->epoch;                         // launch shapes changed: recapture
+    return PG_OK;
+}
 
 }  // extern "C"
 
@@ -517,6 +618,14 @@ int pg_internal_seqs(const pg_ctx *c, const uint8_t **rseq, const uint64_t **rof
 }
 
 int pg_internal_fail(int code, const char *msg) { return fail(code, "%s", msg); }
+
+// internal: the context's substitution table on the device (25 x 25 int8)
+int pg_internal_score(const pg_ctx *c, const int8_t **d_sm)
+{
+    if (!c || !c->d_sm) return fail(PG_ERR_STATE, "no context");
+    *d_sm = c->d_sm;
+    return PG_OK;
+}
 
 extern "C" {
 

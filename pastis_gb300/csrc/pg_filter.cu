@@ -13,10 +13,15 @@
 // k-mer count c, k-mer score s, seeds (r0, c0), (r1, c1)), fixed scaling:
 //   0 log2(1+c)/4       1 s/32             2 [c >= 2]
 //   3 (c0-r0)/L         4 (c1-r1)/L*[c>=2]  5 |(c0-r0)-(c1-r1)|/L*[c>=2]
-//   6 r0/m              7 c0/n             8 |r0/m - c0/n|
+//   6 r0/m              7 c0/n             8 best seed diagonal window (below)
 //   9 log2(m)/12       10 log2(n)/12      11 |log2(m/n)|
 //  12..15 |fraction difference| of the two sequences in four residue groups:
 //         hydrophobic AVLIMFWC, polar NQSTYGP, positive RKH, negative DE
+// Seed diagonal window: the mean substitution score over the 64 positions of
+// a seed's diagonal from 32 before its start (positions outside either
+// sequence skipped), divided by 4; the larger of the two seeds when the pair
+// has two different ones.  It is the ungapped check BLAST-style seeders make
+// before a gapped extension.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -33,6 +38,7 @@ int pg_internal_seqs(const pg_ctx *c, const uint8_t **rseq, const uint64_t **rof
                      const uint8_t **cseq, const uint64_t **coffs, uint64_t *nc, int *device,
                      void **stream, int *mode);
 int pg_internal_fail(int code, const char *msg);
+int pg_internal_score(const pg_ctx *c, const int8_t **d_sm);
 
 namespace {
 
@@ -181,9 +187,26 @@ __global__ void k_composition(const uint8_t *seq, const uint64_t *offs, uint64_t
     }
 }
 
+constexpr int WIN_BEFORE = 32, WIN_LEN = 64;
+
+__device__ float diag_window(const uint8_t *V, int m, const uint8_t *H, int n, int r0, int c0,
+                             const int8_t *sm)
+{
+    int s = 0, cnt = 0;
+    for (int t = -WIN_BEFORE; t < WIN_LEN - WIN_BEFORE; ++t) {
+        const int i = r0 + t, j = c0 + t;
+        if (i < 0 || j < 0 || i >= m || j >= n) continue;
+        s += sm[V[i] * PG_NRES + H[j]];
+        ++cnt;
+    }
+    return cnt ? (float)s / (4.f * (float)cnt) : 0.f;
+}
+
 __global__ void k_features(const pg_pair *pairs, uint64_t n, uint64_t roff, uint64_t coff,
-                           const uint64_t *roffs, uint64_t nr, const uint64_t *coffs, uint64_t nc,
-                           const float4 *rcomp, const float4 *ccomp, __nv_bfloat16 *X, int *status)
+                           const uint8_t *rseq, const uint64_t *roffs, uint64_t nr,
+                           const uint8_t *cseq, const uint64_t *coffs, uint64_t nc,
+                           const int8_t *sm, const float4 *rcomp, const float4 *ccomp,
+                           __nv_bfloat16 *X, int *status)
 {
     for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n;
          p += (uint64_t)gridDim.x * blockDim.x) {
@@ -207,7 +230,14 @@ __global__ void k_features(const pg_pair *pairs, uint64_t n, uint64_t roff, uint
             f[5] = two ? fabsf(d0 - d1) : 0.f;
             f[6] = (float)pr.rs0 / mm;
             f[7] = (float)pr.cs0 / n1;
-            f[8] = fabsf(f[6] - f[7]);
+            {
+                const uint8_t *V = rseq + roffs[r], *H = cseq + coffs[c];
+                const int mi = (int)(roffs[r + 1] - roffs[r]), ni = (int)(coffs[c + 1] - coffs[c]);
+                float w = diag_window(V, mi, H, ni, pr.rs0, pr.cs0, sm);
+                if (two && (pr.rs1 != pr.rs0 || pr.cs1 != pr.cs0))
+                    w = fmaxf(w, diag_window(V, mi, H, ni, pr.rs1, pr.cs1, sm));
+                f[8] = w;
+            }
             f[9] = log2f(mm) * (1.f / 12.f);
             f[10] = log2f(n1) * (1.f / 12.f);
             f[11] = fabsf(log2f(mm / n1));
@@ -590,6 +620,9 @@ int pg_filter_features(pg_filter *f, pg_ctx *ctx, const pg_pair *d_pairs, uint64
     void *cst;
     int rc = pg_internal_seqs(ctx, &rseq, &roffs, &nr, &cseq, &coffs, &nc, &dev, &cst, &mode);
     if (rc) return rc;
+    const int8_t *d_sm = nullptr;
+    rc = pg_internal_score(ctx, &d_sm);
+    if (rc) return rc;
     FCU(cudaSetDevice(f->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : (cudaStream_t)cst;
     if (nr > f->comp_cap_r) {
@@ -606,8 +639,9 @@ int pg_filter_features(pg_filter *f, pg_ctx *ctx, const pg_pair *d_pairs, uint64
     k_composition<<<grid, 256, 0, st>>>(rseq, roffs, nr, f->d_rcomp);
     k_composition<<<grid, 256, 0, st>>>(cseq, coffs, nc, f->d_ccomp);
     FCU(cudaMemsetAsync(f->d_status, 0, sizeof(int), st));
-    if (n) k_features<<<grid, 256, 0, st>>>(d_pairs, n, bl_roffset, bl_coffset, roffs, nr, coffs, nc,
-                                           f->d_rcomp, f->d_ccomp, (__nv_bfloat16 *)d_features, f->d_status);
+    if (n) k_features<<<grid, 256, 0, st>>>(d_pairs, n, bl_roffset, bl_coffset, rseq, roffs, nr,
+                                           cseq, coffs, nc, d_sm, f->d_rcomp, f->d_ccomp,
+                                           (__nv_bfloat16 *)d_features, f->d_status);
     FCU(cudaGetLastError());
     int status = 0;
     FCU(cudaMemcpyAsync(&status, f->d_status, sizeof status, cudaMemcpyDeviceToHost, st));

@@ -68,6 +68,7 @@ struct KParams {
     int gring_w;
     unsigned int *sched = nullptr;   // [0, NBUCKET) bucket sizes, [NBUCKET, 2*NBUCKET) cursors
     const uint32_t *order = nullptr; // pair taken as the t-th task by k_ga / k_sw (null: t)
+    int rows_cap = 8;                // cap on DP rows per lane (tuning)
 };
 
 __device__ __forceinline__ void load_sm(int *ssm, const int8_t *sm)
@@ -281,9 +282,9 @@ template <class S>
 __host__ __device__ constexpr int dp_rows_max() { return sizeof(S) > 4 ? 4 : 8; }
 
 template <class S>
-__host__ __device__ __forceinline__ int dp_rows_per_lane(int m)
+__host__ __device__ __forceinline__ int dp_rows_per_lane(int m, int cap = 8)
 {
-    constexpr int RMAX = dp_rows_max<S>();
+    const int RMAX = cap < dp_rows_max<S>() ? (cap < 1 ? 1 : cap) : dp_rows_max<S>();
     const int stripes = m > 0 ? (m + 32 * RMAX - 1) / (32 * RMAX) : 1;
     const int r = (m + 32 * stripes - 1) / (32 * stripes);
     return r < 1 ? 1 : r;
@@ -291,11 +292,12 @@ __host__ __device__ __forceinline__ int dp_rows_per_lane(int m)
 
 template <class S, int TIE>
 __device__ __forceinline__ DpOut<S> dp_dispatch(const uint8_t *V, int m, const uint8_t *Hs, int n,
-                                                const int *ssm, uint2 *prof, int go, int ge, void *bnd)
+                                                const int *ssm, uint2 *prof, int go, int ge, void *bnd,
+                                                int cap = 8)
 {
     Edge<S> *b = (Edge<S> *)bnd;
     constexpr int RM = dp_rows_max<S>();
-    switch (dp_rows_per_lane<S>(m)) {
+    switch (dp_rows_per_lane<S>(m, cap)) {
     case 1: return dp_warp<S, TIE, 1>(V, m, Hs, n, ssm, prof, go, ge, b);
     case 2: return dp_warp<S, TIE, 2>(V, m, Hs, n, ssm, prof, go, ge, b);
     case 3: return dp_warp<S, TIE, 3>(V, m, Hs, n, ssm, prof, go, ge, b);
@@ -329,14 +331,14 @@ __device__ __forceinline__ int pair_bucket(const KParams &kp, uint64_t p)
         m = r.ev - r.bv;
         n = r.eh - r.bh;
         if (m <= 0 || n <= 0) return BUCKET_NONE;
-        if (m > S1::MAXSIDE || n > S1::MAXSIDE) return 4 - dp_rows_per_lane<S2>(m);   // 0..3
-        return 12 - dp_rows_per_lane<S1>(m);                                           // 4..11
+        if (m > S1::MAXSIDE || n > S1::MAXSIDE) return 4 - dp_rows_per_lane<S2>(m, kp.rows_cap);   // 0..3
+        return 12 - dp_rows_per_lane<S1>(m, kp.rows_cap);                                           // 4..11
     }
     const pg_pair pr = kp.pairs[p];
     const uint8_t *V, *Hs;
     if (!pair_seqs(kp, pr, V, m, Hs, n) || m == 0 || n == 0) return BUCKET_NONE;
-    if (m > L1::MAXSIDE || n > L1::MAXSIDE) return 4 - dp_rows_per_lane<L2>(m);        // 0..3
-    return 8 - dp_rows_per_lane<L1>(m);                                                // 4..7
+    if (m > L1::MAXSIDE || n > L1::MAXSIDE) return 4 - dp_rows_per_lane<L2>(m, kp.rows_cap);        // 0..3
+    return 8 - dp_rows_per_lane<L1>(m, kp.rows_cap);                                                // 4..7
 }
 
 // bucket sizes
@@ -438,10 +440,10 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga(const KParams kp)
             int score;
             uint32_t M, D, G;
             if (rm <= S1::MAXSIDE && rn <= S1::MAXSIDE) {
-                const DpOut<S1> d = dp_dispatch<S1, TIE>(V + bv, rm, Hs + bh, rn, ssm, prof, kp.go, kp.ge, bnd);
+                const DpOut<S1> d = dp_dispatch<S1, TIE>(V + bv, rm, Hs + bh, rn, ssm, prof, kp.go, kp.ge, bnd, kp.rows_cap);
                 score = d.score; M = d.st.M(); D = d.st.D(); G = d.st.G();
             } else {
-                const DpOut<S2> d = dp_dispatch<S2, TIE>(V + bv, rm, Hs + bh, rn, ssm, prof, kp.go, kp.ge, bnd);
+                const DpOut<S2> d = dp_dispatch<S2, TIE>(V + bv, rm, Hs + bh, rn, ssm, prof, kp.go, kp.ge, bnd, kp.rows_cap);
                 score = d.score; M = d.st.M(); D = d.st.D(); G = d.st.G();
             }
             exec += area;
@@ -500,11 +502,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_sw(const KParams kp)
         int score = 0, have = 0, ei = 0, ej = 0, i0 = 0, j0 = 0;
         uint32_t M = 0, D = 0, G = 0;
         if (m <= L1::MAXSIDE && n <= L1::MAXSIDE) {
-            const DpOut<L1> d = dp_dispatch<L1, TIE>(V, m, Hs, n, ssm, prof, kp.go, kp.ge, bnd);
+            const DpOut<L1> d = dp_dispatch<L1, TIE>(V, m, Hs, n, ssm, prof, kp.go, kp.ge, bnd, kp.rows_cap);
             score = d.score; have = d.have; ei = d.ei; ej = d.ej;
             M = d.st.M(); D = d.st.D(); G = d.st.G(); i0 = d.st.i0(); j0 = d.st.j0();
         } else {
-            const DpOut<L2> d = dp_dispatch<L2, TIE>(V, m, Hs, n, ssm, prof, kp.go, kp.ge, bnd);
+            const DpOut<L2> d = dp_dispatch<L2, TIE>(V, m, Hs, n, ssm, prof, kp.go, kp.ge, bnd, kp.rows_cap);
             score = d.score; have = d.have; ei = d.ei; ej = d.ej;
             M = d.st.M(); D = d.st.D(); G = d.st.G(); i0 = d.st.i0(); j0 = d.st.j0();
         }

@@ -38,6 +38,16 @@ def test_struct_layouts(native):
     assert capi.PAIR_DTYPE == oracle.PAIR_DTYPE
     assert capi.RESULT_DTYPE == oracle.RESULT_DTYPE
     assert ctypes.sizeof(capi.Config) == 64
+    assert ctypes.sizeof(capi.Tuning) == 32
+
+
+def test_tuning_defaults_without_gpu(native):
+    """pg_tuning_default: occupancy-limited grids, bucketed order, 8 rows per
+    lane, no graph."""
+    from pastis_gb300 import capi
+    t = capi.default_tuning()
+    assert t.as_dict() == {"dp_blocks_per_sm": 0, "xd_blocks_per_sm": 0, "bucket_order": 1,
+                           "rows_max": 8, "graph": 0}
 
 
 def test_defaults_and_errors_without_gpu(native):

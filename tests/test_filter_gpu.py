@@ -118,3 +118,35 @@ def test_trained_filter_beats_kmer_prune(native):
     assert m["test"]["kept_fraction"] < m["kmer_rule_kept_at_same_recall"]
     f.close()
     ctx.close()
+
+
+def test_features_match_oracle(native):
+    """k_features against the float32 restatement in oracle/mlp_oracle.py,
+    after bf16 rounding: at most one bf16 step apart (log2 may differ in the
+    last float32 bit), and identical for almost every value."""
+    import torch
+    from oracle import mlp_oracle as M
+    from oracle import oracle as O
+    from pastis_gb300 import capi, synth
+    from pastis_gb300.filter import Filter
+    w = synth.generate("xdrop1m", seed=44, scale=0.003)
+    ctx = capi.Context(capi.config(capi.MODE_XDROP))
+    ctx.set_seqs(0, w.ascii, w.offs)
+    ctx.share_row_seqs()
+    n = len(w.pairs)
+    d_pairs = torch.from_numpy(w.pairs.view(np.uint8).copy()).cuda()
+    feats = torch.empty(n * 32, dtype=torch.uint8, device="cuda:0")
+    f = Filter(0, seed=1)
+    f.features(ctx, d_pairs.data_ptr(), n, feats.data_ptr())
+    torch.cuda.synchronize()
+    got = feats.cpu().numpy().view(np.uint16).reshape(n, 16).astype(np.int64)
+    ref = M.features(w.pairs, w.seq, w.offs, O.blosum62().reshape(-1))
+    ref_bits = (M.bf16(ref).astype(np.float32).view(np.uint32) >> 16).astype(np.int64)
+    diff = np.abs(got - ref_bits)
+    assert diff.max() <= 1
+    assert (diff == 0).mean() > 0.99
+    # the seed window separates homologs from random pairs on this generator
+    win = ref[:, 8]
+    assert win[w.homolog == 1].mean() > win[w.homolog == 0].mean() + 0.2
+    f.close()
+    ctx.close()

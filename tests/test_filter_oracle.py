@@ -33,3 +33,26 @@ def test_bf16_rounding():
     assert abs(r[3] + 3.140625) < 1e-9
     bits = r.astype(np.float32).view(np.uint32)
     assert (bits & 0xFFFF == 0).all()
+
+
+def test_feature_restatement_by_hand():
+    """Two identical 40-residue sequences, seed at (5, 5): the diagonal window
+    [5 - 32, 5 + 32) covers positions 0..36, so feature 8 is their mean
+    self-score / 4."""
+    from oracle import mlp_oracle as M
+    from oracle import oracle as O
+    from pastis_gb300 import capi
+    sm = O.blosum62().reshape(-1)
+    rng = np.random.default_rng(3)
+    s = rng.integers(0, 20, 40)
+    codes = np.concatenate([s, s]).astype(np.uint8)
+    offs = np.array([0, 40, 80], dtype=np.uint64)
+    pr = np.zeros(1, dtype=capi.PAIR_DTYPE)
+    pr["row"], pr["col"], pr["rs0"], pr["cs0"], pr["count"], pr["score"] = 0, 1, 5, 5, 1, 20
+    f = M.features(pr, codes, offs, sm)[0]
+    self_score = sum(int(sm[a * 25 + a]) for a in s[:37])
+    assert np.isclose(f[8], self_score / (4.0 * 37))
+    assert f[3] == 0 and f[11] == 0 and np.all(f[12:] == 0)
+    assert np.isclose(f[0], np.log2(2.0) / 4) and np.isclose(f[1], 20 / 32)
+    comp = M.composition(codes, offs)
+    assert np.allclose(comp.sum(axis=1), 1.0)

@@ -233,3 +233,46 @@ def test_cpp_driver_on_gpu(sw_small, oracle_mod):
     assert st["nnz_aln"] == st2["nnz_aln"] and st["batches"] == 4
     assert (r_gpu == r_cpu).all() and (c_gpu == c_cpu).all()
     assert (v_gpu["score_aln"].view(np.uint32) == v_cpu["score_aln"].view(np.uint32)).all()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_tuning_and_graph_replay_keep_results(native, oracle_mod, mode):
+    """Every launch tuning (grid sizes, bucket order, rows per lane, graph
+    capture and replay) gives the oracle's results byte for byte."""
+    import torch
+    from pastis_gb300 import capi, synth
+    w = synth.generate("sw100k" if mode == capi.MODE_SW else "xdrop1m", seed=211,
+                       scale=0.01 if mode == capi.MODE_SW else 0.004)
+    cfg = capi.config(mode)
+    ctx = capi.Context(cfg)
+    ctx.set_seqs(0, w.ascii, w.offs)
+    ctx.share_row_seqs()
+    O = oracle_mod
+    codes = O.encode(bytes(w.ascii))
+    exp = O.batch(mode, codes, w.offs, codes, w.offs, w.pairs, oracle_params(O, cfg))
+    kernels = 5 if mode == capi.MODE_XDROP else 3
+    for t in ({}, {"bucket_order": 0}, {"rows_max": 3}, {"rows_max": 1, "dp_blocks_per_sm": 1},
+              {"xd_blocks_per_sm": 2}, {"graph": 1}, {"graph": 1, "bucket_order": 0}):
+        ctx.set_tuning(capi.default_tuning(), **t)
+        for rep in range(2):                 # the second call replays the graph
+            got = ctx.align(w.pairs)
+            assert_same(got, exp, w.pairs)
+        want = kernels if t.get("bucket_order", 1) else kernels - 2
+        assert ctx.last_launches() == want, t
+    # device entry point with graph replay on a caller stream
+    n = len(w.pairs)
+    d_pairs = torch.from_numpy(w.pairs.view(np.uint8).copy()).cuda()
+    d_out = torch.empty(n * capi.RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda:0")
+    s = torch.cuda.Stream()
+    for _ in range(3):
+        d_out.zero_()
+        torch.cuda.synchronize()
+        ctx.align_device(d_pairs.data_ptr(), n, d_out.data_ptr(), s.cuda_stream)
+        s.synchronize()
+        got = np.frombuffer(d_out.cpu().numpy().tobytes(), dtype=capi.RESULT_DTYPE)
+        assert_same(got, exp, w.pairs)
+    with pytest.raises(capi.PgError):
+        ctx.set_tuning(rows_max=9)
+    with pytest.raises(capi.PgError):
+        ctx.set_tuning(graph=2)
+    ctx.close()
