@@ -32,7 +32,7 @@ extern "C" {
 #define PG_ERR_OOM      -3   /* device or pinned-host allocation failed */
 #define PG_ERR_TIMEOUT  -4   /* a bounded device wait ran out (status word set) */
 #define PG_ERR_STATE    -5   /* call order (e.g. pg_align before pg_set_seqs) */
-#define PG_ERR_RANGE    -6   /* a sequence is longer than 65535 residues */
+#define PG_ERR_RANGE    -6   /* a size limit: sequence over 65535 residues, output capacity, product bound */
 #define PG_ERR_NODEV    -7   /* no CUDA device / device id out of range */
 
 /* ---- alignment modes (params_t::PwAln, inc/Types.hpp:52-59) */
@@ -232,6 +232,53 @@ int pg_align_sw_noalloc(const pg_config *cfg,
                         uint32_t max_col_len, const pg_pair *d_pairs, uint64_t n,
                         uint64_t bl_roffset, uint64_t bl_coffset, pg_result *d_out,
                         void *stream);
+
+/* ---- candidate generation: the k-mer SpGEMM C = A·Aᵀ that feeds the aligner
+ * (src/kmer/KmerOps.cpp:31-245 builds A, sim_search.cpp:154-157 multiplies,
+ * inc/sr.hpp:30-117 is the KmerIntersectLoc semiring).  A holds one entry per
+ * k-mer occurrence (code over the alphabet, offset, self score of the k-mer
+ * over the alphabet's representative letters); C(r, c) gets
+ *   count = occurrence pairs sharing a k-mer (16-bit, wrapping as ushort does),
+ *   score = the largest shared k-mer self score,
+ *   first  = (row offset, col offset) of the smallest (code, row off, col off),
+ *   second = the same of the largest; (0, 0) when count == 1.
+ * Pairs come out block-relative (row - row_begin, col - col_begin) in column-
+ * major order (by col, then row), as PASTIS forms its tuples. */
+#define PG_ALPH_PROTEIN   0   /* 25 letters ARNDCQEGHILKMFPSTWYVBZX*J       */
+#define PG_ALPH_MURPHY10  1   /* murphy10 groups, 15 codes (inc/Alphabet.hpp:83-104) */
+
+#define PG_PRUNE_NONE     0   /* keep every pair, the diagonal included           */
+#define PG_PRUNE_EVEN_ODD 1   /* one of (r,c)/(c,r) by parity, r != c (sim_search.cpp:172-186) */
+#define PG_PRUNE_UPPER    2   /* strict upper triangle r < c (sim_search.cpp:403-412) */
+
+typedef struct pg_kmer_config {
+    int32_t  k;              /* k-mer length (--kmer-len, default 6)             */
+    int32_t  stride;         /* k-mer stride (--kmer-stride, default 1)          */
+    int32_t  alphabet;       /* PG_ALPH_*                                        */
+    int32_t  prune;          /* PG_PRUNE_*                                       */
+    int32_t  ckthr;          /* drop pairs with count <= ckthr (0 keeps all)     */
+    int32_t  mosthr;         /* drop pairs with score <= mosthr                  */
+    uint64_t max_products;   /* occurrence pairs one call may hold; 0 = 2^31     */
+} pg_kmer_config;            /* 32 bytes */
+
+void pg_kmer_config_default(pg_kmer_config *kc);
+/* Candidate pairs of rows [row_begin, row_end) x columns [col_begin, col_end)
+ * of the context's row and column sequences into d_out (device, cap records).
+ * *n_out = pairs found.  PG_ERR_RANGE when they exceed cap (d_out untouched,
+ * *n_out = the count needed) or the occurrence pairs exceed max_products
+ * (*n_out = 0); PG_ERR_ARG when alphabet_size^k exceeds 2^31 (the reference's
+ * own limit) or a range is out of bounds.  Synchronous. */
+int pg_candidates(pg_ctx *ctx, const pg_kmer_config *kc, uint64_t row_begin, uint64_t row_end,
+                  uint64_t col_begin, uint64_t col_end, pg_pair *d_out, uint64_t cap,
+                  uint64_t *n_out, void *stream);
+
+/* The similarity-matrix triples of an aligned batch (src/sim_search.cpp:221-232
+ * after the score_aln == 0 prune of src/DistPWRunner.cpp:149-153):
+ * (row + bl_roffset, col + bl_coffset, score_aln) of every pair whose score_aln
+ * is not 0, in batch order, into device arrays of n entries.  Synchronous. */
+int pg_triples(const pg_pair *d_pairs, const pg_result *d_res, uint64_t n,
+               uint64_t bl_roffset, uint64_t bl_coffset, uint64_t *d_rows, uint64_t *d_cols,
+               float *d_vals, uint64_t *n_out, void *stream);
 
 /* Measured throughput of the DPX add-max instruction on a device, in
  * instructions per second over all SMs (the roofline of the DP kernels). */

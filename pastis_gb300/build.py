@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC]
-CUDA_UNITS = ("pg_api.cu", "pg_filter.cu")
+CUDA_UNITS = ("pg_api.cu", "pg_filter.cu", "pg_kmer.cu")
 
 
 def _steps():
@@ -46,6 +46,7 @@ def _steps():
              + ["-L", BUILD, "-lpastis_gb300", "-Wl,-rpath,$ORIGIN"],
              host_src + [os.path.join(BUILD, "libpastis_gb300.so"),
                          os.path.join(INC, "pastis_gb300_pwalign.hpp"),
+                         os.path.join(INC, "pastis_gb300_host.h"),
                          os.path.join(INC, "pastis_gb300.h")])]
     return [compile_jobs, link, host]
 

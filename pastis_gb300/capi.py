@@ -48,12 +48,13 @@ EXPORTS = {
                            "pg_filter_destroy", "pg_filter_nparams", "pg_filter_params",
                            "pg_filter_features", "pg_filter_predict", "pg_filter_gradients",
                            "pg_filter_train_step", "pg_align_filtered", "pg_tuning_default",
-                           "pg_get_tuning", "pg_set_tuning"],
+                           "pg_get_tuning", "pg_set_tuning", "pg_kmer_config_default",
+                           "pg_candidates", "pg_triples"],
     "libpastis_synth.so": ["pg_synth_generate", "pg_synth_free", "pg_synth_nseqs",
                            "pg_synth_nres", "pg_synth_npairs", "pg_synth_seq", "pg_synth_offs",
                            "pg_synth_family", "pg_synth_pairs", "pg_synth_homolog",
                            "pg_synth_spurious"],
-    "libpastis_host.so": ["pgh_pw_aln_batch", "pgh_last_error"],
+    "libpastis_host.so": ["pgh_pw_aln_batch", "pgh_last_error", "pgh_write_mm"],
 }
 
 
@@ -80,6 +81,46 @@ class Tuning(ctypes.Structure):
 
 
 _libs = {}
+
+
+ALPH_PROTEIN, ALPH_MURPHY10 = 0, 1
+PRUNE_NONE, PRUNE_EVEN_ODD, PRUNE_UPPER = 0, 1, 2
+
+
+class KmerConfig(ctypes.Structure):
+    """pg_kmer_config: k-mer candidate generation (the SpGEMM and its semiring)."""
+    _fields_ = [("k", ctypes.c_int32), ("stride", ctypes.c_int32), ("alphabet", ctypes.c_int32),
+                ("prune", ctypes.c_int32), ("ckthr", ctypes.c_int32), ("mosthr", ctypes.c_int32),
+                ("max_products", ctypes.c_uint64)]
+
+
+def kmer_config(**fields):
+    kc = KmerConfig()
+    load().pg_kmer_config_default(ctypes.byref(kc))
+    for k, v in fields.items():
+        setattr(kc, k, v)
+    return kc
+
+
+def triples_device(d_pairs, d_res, n, roff, coff, d_rows, d_cols, d_vals, stream=None):
+    """Similarity triples (row, col, score_aln != 0) of an aligned batch, on
+    the device; returns how many were written."""
+    cnt = ctypes.c_uint64()
+    _check(load().pg_triples(d_pairs, d_res, n, roff, coff, d_rows, d_cols, d_vals,
+                             ctypes.byref(cnt), stream))
+    return int(cnt.value)
+
+
+def write_mm(path, nrows, ncols, rows, cols, vals):
+    """Matrix Market file of similarity triples (host arrays)."""
+    rows = np.ascontiguousarray(rows, dtype=np.uint64)
+    cols = np.ascontiguousarray(cols, dtype=np.uint64)
+    vals = np.ascontiguousarray(vals, dtype=np.float32)
+    lib = load("libpastis_host.so")
+    rc = lib.pgh_write_mm(str(path).encode(), nrows, ncols, rows.ctypes.data, cols.ctypes.data,
+                          vals.ctypes.data, len(rows))
+    if rc != PG_OK:
+        raise PgError(rc, lib.pgh_last_error().decode(errors="replace"))
 
 
 def default_tuning():
@@ -119,6 +160,11 @@ def _declare(name, lib):
         lib.pg_exec_cells_split.argtypes = [vp, vp]
         lib.pg_kernel_ms.argtypes = [vp, vp]
         lib.pg_dpx_peak.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
+        lib.pg_kmer_config_default.argtypes = [vp]
+        lib.pg_kmer_config_default.restype = None
+        lib.pg_candidates.argtypes = [vp, vp, u64, u64, u64, u64, vp, u64,
+                                      ctypes.POINTER(u64), vp]
+        lib.pg_triples.argtypes = [vp, vp, u64, u64, u64, vp, vp, vp, ctypes.POINTER(u64), vp]
         lib.pg_tuning_default.argtypes = [vp]
         lib.pg_tuning_default.restype = None
         lib.pg_get_tuning.argtypes = [vp, vp]
@@ -154,6 +200,7 @@ def _declare(name, lib):
         lib.pg_synth_free.restype = None
     elif name == "libpastis_host.so":
         lib.pgh_last_error.restype = ctypes.c_char_p
+        lib.pgh_write_mm.argtypes = [ctypes.c_char_p, u64, u64, vp, vp, vp, u64]
 
 
 class PgError(RuntimeError):
@@ -260,6 +307,31 @@ class Context:
         v = (ctypes.c_float * 2)()
         _check(self.lib.pg_kernel_ms(self.h, v))
         return float(v[0]), float(v[1])
+
+    def candidates_device(self, kc, rows, cols, d_out, cap, stream=None):
+        """Candidate pairs of the block rows x cols (ranges) into a device
+        buffer; returns how many were written."""
+        n = ctypes.c_uint64()
+        _check(self.lib.pg_candidates(self.h, ctypes.byref(kc), rows[0], rows[1], cols[0], cols[1],
+                                      d_out, cap, ctypes.byref(n), stream))
+        return int(n.value)
+
+    def candidates(self, kc, rows, cols):
+        """The same into host memory (sizes the output with a first call)."""
+        import torch
+        dev = self.cfg.device
+        n = ctypes.c_uint64()
+        rc = self.lib.pg_candidates(self.h, ctypes.byref(kc), rows[0], rows[1], cols[0], cols[1],
+                                    None, 0, ctypes.byref(n), None)
+        if rc not in (PG_OK, PG_ERR_RANGE) or (rc == PG_ERR_RANGE and n.value == 0):
+            _check(rc)
+        cnt = int(n.value)
+        if cnt == 0:
+            return np.zeros(0, dtype=PAIR_DTYPE)
+        buf = torch.empty(cnt * PAIR_DTYPE.itemsize, dtype=torch.uint8, device="cuda:%d" % dev)
+        got = self.candidates_device(kc, rows, cols, buf.data_ptr(), cnt)
+        return np.frombuffer(buf[:got * PAIR_DTYPE.itemsize].cpu().numpy().tobytes(),
+                             dtype=PAIR_DTYPE).copy()
 
     def get_tuning(self):
         t = Tuning()

@@ -4,26 +4,14 @@
 // pgh_pw_aln_batch runs pw_aln_batch (src/DistPWRunner.cpp:25-165) on one
 // rank's block with either the GPU aligner or a caller-supplied aligner
 // callback (used to test the driver's pruning and batching without a GPU).
+#include <cstdio>
 #include <cstring>
 #include <exception>
 #include <string>
 
 #include "pastis_gb300.h"
+#include "pastis_gb300_host.h"
 #include "pastis_gb300_pwalign.hpp"
-
-extern "C" {
-
-// callback aligner: fills score_aln[i] for pairs[0..n)
-typedef int (*pgh_align_cb)(const pg_pair *pairs, uint64_t n, uint64_t bl_roff, uint64_t bl_coff,
-                            float *score_aln, void *user);
-
-int pgh_pw_aln_batch(int mode, const pg_config *cfg,
-                     const char *rres, const uint64_t *roffs, uint64_t nr,
-                     const char *cres, const uint64_t *coffs, uint64_t nc,
-                     uint64_t nnz, uint64_t *rows, uint64_t *cols, void *vals,
-                     uint64_t bl_roff, uint64_t bl_coff, uint64_t batch_sz, int ckthr, float mosthr,
-                     pgh_align_cb cb, void *cb_user, uint64_t *out_stats, double *out_seconds);
-}
 
 namespace {
 
@@ -155,6 +143,45 @@ extern "C" int pgh_pw_aln_batch(int mode, const pg_config *cfg,
         g_host_err = e.what();
         return PG_ERR_STATE;
     }
+}
+
+extern "C" int pgh_write_mm(const char *path, uint64_t nrows, uint64_t ncols, const uint64_t *rows,
+                            const uint64_t *cols, const float *vals, uint64_t n)
+{
+    if (!path || (n && (!rows || !cols || !vals))) {
+        g_host_err = "pgh_write_mm: bad argument";
+        return PG_ERR_ARG;
+    }
+    FILE *f = std::fopen(path, "w");
+    if (!f) {
+        g_host_err = std::string("pgh_write_mm: cannot open ") + path;
+        return PG_ERR_ARG;
+    }
+    std::fprintf(f, "%%%%MatrixMarket matrix coordinate real general\n");
+    std::fprintf(f, "%llu %llu %llu\n", (unsigned long long)nrows, (unsigned long long)ncols,
+                 (unsigned long long)n);
+    char buf[32];
+    for (uint64_t i = 0; i < n; ++i) {
+        if (rows[i] >= nrows || cols[i] >= ncols) {
+            std::fclose(f);
+            g_host_err = "pgh_write_mm: triple out of range";
+            return PG_ERR_ARG;
+        }
+        // shortest %g form that reads back to the same float
+        for (int prec = 6; prec <= 9; ++prec) {
+            std::snprintf(buf, sizeof buf, "%.*g", prec, (double)vals[i]);
+            if (std::strtof(buf, nullptr) == vals[i]) break;
+        }
+        std::fprintf(f, "%llu %llu %s\n", (unsigned long long)rows[i] + 1,
+                     (unsigned long long)cols[i] + 1, buf);
+    }
+    const bool ok = std::fflush(f) == 0;
+    std::fclose(f);
+    if (!ok) {
+        g_host_err = "pgh_write_mm: write failed";
+        return PG_ERR_ARG;
+    }
+    return PG_OK;
 }
 
 extern "C" const char *pgh_last_error(void) { return g_host_err.c_str(); }

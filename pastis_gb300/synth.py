@@ -12,6 +12,8 @@ Workload presets follow the benchmark definitions of this stage:
              1000-5000, min 20
   filter5m   5M pairs of the sw100k generator at a 30 % homolog rate (the
              learned filter's training and evaluation set)
+  manytomany 1M proteins in families of 2-50 at 30-90 % identity; its
+             candidate pairs come from the GPU k-mer SpGEMM, not the generator
 """
 import ctypes
 from dataclasses import dataclass, field
@@ -72,6 +74,9 @@ PRESETS = {
                       len_min=20, len_max=5000, mix_frac=0.2, mix_lo=1000, mix_hi=5000,
                       id_lo=0.30, id_hi=0.80, homolog_frac=0.5, k=6, alph=0, fam_min=6,
                       fam_max=6),
+    "manytomany": dict(nseqs=1_000_000, npairs=1_000, len_median=250.0, len_sigma=0.5,
+                       len_min=30, len_max=1000, mix_frac=0.0, mix_lo=0, mix_hi=0, id_lo=0.30,
+                       id_hi=0.90, homolog_frac=0.5, k=6, alph=0, fam_min=2, fam_max=50),
     "filter5m": dict(nseqs=1_000_000, npairs=5_000_000, len_median=250.0, len_sigma=0.5,
                      len_min=30, len_max=1000, mix_frac=0.0, mix_lo=0, mix_hi=0, id_lo=0.30,
                      id_hi=0.80, homolog_frac=0.3, k=6, alph=0, fam_min=6, fam_max=6),

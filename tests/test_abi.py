@@ -19,8 +19,10 @@ def _declared(header):
 
 def test_headers_match_exports(native):
     from pastis_gb300 import capi
-    decl = _declared("pastis_gb300.h") | _declared("pastis_gb300_synth.h")
-    exported = set(capi.EXPORTS["libpastis_gb300.so"]) | set(capi.EXPORTS["libpastis_synth.so"])
+    decl = (_declared("pastis_gb300.h") | _declared("pastis_gb300_synth.h")
+            | _declared("pastis_gb300_host.h"))
+    exported = (set(capi.EXPORTS["libpastis_gb300.so"]) | set(capi.EXPORTS["libpastis_synth.so"])
+                | set(capi.EXPORTS["libpastis_host.so"]))
     assert decl == exported, (decl ^ exported)
 
 

@@ -102,3 +102,22 @@ def test_empty_block(native):
     r2, c2, v2, st = capi.pw_aln_batch(capi.MODE_SW, [], [], np.zeros(0, capi.KMERLIGHT_DTYPE),
                                       res, offs, callback=lambda *a: called.append(1))
     assert st["nnz_in"] == 0 and st["batches"] == 0 and not called
+
+
+def test_matrix_market_writer(native, tmp_path):
+    """1-based coordinates, the header PASTIS's --align-file carries, values
+    that read back to the same float; out-of-range triples rejected."""
+    import numpy as np
+    import pytest
+    from pastis_gb300 import capi
+    path = tmp_path / "sim.mtx"
+    vals = np.array([0.5, 0.123456789, 1.0 / 3.0], dtype=np.float32)
+    capi.write_mm(path, 10, 12, [0, 9, 3], [11, 0, 3], vals)
+    lines = path.read_text().splitlines()
+    assert lines[0] == "%%MatrixMarket matrix coordinate real general"
+    assert lines[1] == "10 12 3"
+    got = [ln.split() for ln in lines[2:]]
+    assert [(int(a), int(b)) for a, b, _ in got] == [(1, 12), (10, 1), (4, 4)]
+    assert np.array_equal(np.array([float(v) for _, _, v in got], dtype=np.float32), vals)
+    with pytest.raises(capi.PgError):
+        capi.write_mm(path, 10, 12, [10], [0], [1.0])
