@@ -572,6 +572,13 @@ def run_manytomany(args, rank, world, local_rank):
                 m = min(bsz, n - s)
                 yield roff, coff, buf[s * P:(s + m) * P], m
 
+    # warm-up: the first batch of each path once, untimed
+    for roff, coff, pb, m in batches():
+        ctx.align_device(pb.data_ptr(), m, out.data_ptr(), stream.cuda_stream, roff, coff)
+        capi.triples_device(pb.data_ptr(), out.data_ptr(), m, roff, coff, tr.data_ptr(),
+                            tc.data_ptr(), tv.data_ptr(), stream.cuda_stream)
+        break
+
     # 2. plain path: alignment + triples per batch; per-pair pass mask kept for recall
     plain_pass = []
     cells = 0
@@ -579,7 +586,7 @@ def run_manytomany(args, rank, world, local_rank):
     sync()
     t0 = time.perf_counter()
     for roff, coff, pb, m in batches():
-        ctx.align_device(pb.data_ptr(), m, roff, coff, out.data_ptr(), stream.cuda_stream)
+        ctx.align_device(pb.data_ptr(), m, out.data_ptr(), stream.cuda_stream, roff, coff)
         ntrip += capi.triples_device(pb.data_ptr(), out.data_ptr(), m, roff, coff, tr.data_ptr(),
                                      tc.data_ptr(), tv.data_ptr(), stream.cuda_stream)
         res = out[:m * R].view(torch.int32).view(m, R // 4)
@@ -600,8 +607,13 @@ def run_manytomany(args, rank, world, local_rank):
     sample = allp[rng.permutation(len(allp))[:min(len(allp), args.filter_train_pairs)]]
     ws = types.SimpleNamespace(pairs=sample, ascii=w.ascii, offs=w.offs,
                                lengths=w.lengths)
-    f, thr, fm = F.fit(ws, dev, recall=0.997)
+    # label: the plain aligner's own verdict (coverage/ANI filter passed)
+    lab = (ctx.align(sample)["score_aln"] != 0).astype(np.float32)
+    f, thr, fm = F.fit(ws, dev, recall=0.997, labels=lab)
     torch.cuda.set_stream(stream)
+    for roff, coff, pb, m in batches():
+        f.align_filtered(ctx, thr, pb.data_ptr(), m, out.data_ptr(), stream.cuda_stream, roff, coff)
+        break
 
     # 4. filtered path
     fpass = []

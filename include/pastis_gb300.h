@@ -128,6 +128,23 @@ int pg_set_seqs(pg_ctx *ctx, int32_t side, const char *residues,
  * SeqanFullAligner.cpp:82-87). */
 int pg_share_row_seqs(pg_ctx *ctx);
 
+/* Parse a FASTA buffer (host memory, len bytes) on the GPU straight into the
+ * row (side 0) or column (side 1) sequences, as FastaData::FastaData parses a
+ * block (src/FastaData.cpp:13-148): a record starts at the first '>' of a
+ * line, newlines and '*' in sequence text are dropped, 'U'/'u' read as 'T',
+ * and a record with fewer than k residues is removed where the reference
+ * removes it.  *n_kept / *n_removed count records; orig_index (host, optional)
+ * receives the record index of each kept sequence, up to orig_cap entries.
+ * Replaces the host parse and construct_seqs in one step. */
+int pg_set_seqs_fasta(pg_ctx *ctx, int32_t side, const char *fasta, uint64_t len, int32_t k,
+                      uint64_t *n_kept, uint64_t *n_removed, uint64_t *orig_index,
+                      uint64_t orig_cap);
+
+/* Copy one side's resident sequences back (residue codes 0..24, offsets of
+ * n+1 entries); NULL buffers skip the copy, so a first call can size them. */
+int pg_get_seqs(const pg_ctx *ctx, int32_t side, uint8_t *codes, uint64_t *offsets,
+                uint64_t *n, uint64_t *total);
+
 /* Align n pairs in host memory; writes n results to host memory.  Pair i uses
  * row sequence pairs[i].row + bl_roffset and column sequence
  * pairs[i].col + bl_coffset (PWAlign::aln_batch, PWAlign.hpp:47-63).  n == 0

@@ -49,7 +49,7 @@ EXPORTS = {
                            "pg_filter_features", "pg_filter_predict", "pg_filter_gradients",
                            "pg_filter_train_step", "pg_align_filtered", "pg_tuning_default",
                            "pg_get_tuning", "pg_set_tuning", "pg_kmer_config_default",
-                           "pg_candidates", "pg_triples"],
+                           "pg_candidates", "pg_triples", "pg_set_seqs_fasta", "pg_get_seqs"],
     "libpastis_synth.so": ["pg_synth_generate", "pg_synth_free", "pg_synth_nseqs",
                            "pg_synth_nres", "pg_synth_npairs", "pg_synth_seq", "pg_synth_offs",
                            "pg_synth_family", "pg_synth_pairs", "pg_synth_homolog",
@@ -164,6 +164,9 @@ def _declare(name, lib):
         lib.pg_kmer_config_default.restype = None
         lib.pg_candidates.argtypes = [vp, vp, u64, u64, u64, u64, vp, u64,
                                       ctypes.POINTER(u64), vp]
+        lib.pg_set_seqs_fasta.argtypes = [vp, i32, ctypes.c_char_p, u64, i32, ctypes.POINTER(u64),
+                                          ctypes.POINTER(u64), vp, u64]
+        lib.pg_get_seqs.argtypes = [vp, i32, vp, vp, ctypes.POINTER(u64), ctypes.POINTER(u64)]
         lib.pg_triples.argtypes = [vp, vp, u64, u64, u64, vp, vp, vp, ctypes.POINTER(u64), vp]
         lib.pg_tuning_default.argtypes = [vp]
         lib.pg_tuning_default.restype = None
@@ -307,6 +310,27 @@ class Context:
         v = (ctypes.c_float * 2)()
         _check(self.lib.pg_kernel_ms(self.h, v))
         return float(v[0]), float(v[1])
+
+    def set_seqs_fasta(self, side, fasta, k=6):
+        """Parse FASTA text (bytes) on the GPU into one side; returns
+        (kept record indices, removed count)."""
+        fasta = bytes(fasta)
+        nk, nrm = ctypes.c_uint64(), ctypes.c_uint64()
+        cap = fasta.count(b">") + 1
+        orig = np.zeros(cap, dtype=np.uint64)
+        _check(self.lib.pg_set_seqs_fasta(self.h, side, fasta, len(fasta), k, ctypes.byref(nk),
+                                          ctypes.byref(nrm), orig.ctypes.data, cap))
+        return orig[:nk.value].copy(), int(nrm.value)
+
+    def get_seqs(self, side):
+        """(residue codes, offsets) resident for one side."""
+        n, tot = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(self.lib.pg_get_seqs(self.h, side, None, None, ctypes.byref(n), ctypes.byref(tot)))
+        codes = np.zeros(max(1, tot.value), dtype=np.uint8)
+        offs = np.zeros(n.value + 1, dtype=np.uint64)
+        _check(self.lib.pg_get_seqs(self.h, side, codes.ctypes.data, offs.ctypes.data, None,
+                                    None))
+        return codes[:tot.value], offs
 
     def candidates_device(self, kc, rows, cols, d_out, cap, stream=None):
         """Candidate pairs of the block rows x cols (ranges) into a device

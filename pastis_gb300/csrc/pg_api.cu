@@ -568,6 +568,22 @@ int pg_align(pg_ctx *c, const pg_pair *pairs, uint64_t n, uint64_t roff, uint64_
 
 int pg_last_launches(const pg_ctx *c) { return c ? c->last_launches : 0; }
 
+int pg_get_seqs(const pg_ctx *c, int32_t side, uint8_t *codes, uint64_t *offsets, uint64_t *n,
+                uint64_t *total)
+{
+    if (!c || (side != 0 && side != 1)) return fail(PG_ERR_ARG, "pg_get_seqs: bad argument");
+    const Side &s = c->side[side];
+    if (!s.seq) return fail(PG_ERR_STATE, "sequences not set");
+    CU(cudaSetDevice(c->cfg.device));
+    uint64_t tot = 0;
+    CU(cudaMemcpy(&tot, s.offs + s.n, sizeof tot, cudaMemcpyDeviceToHost));
+    if (n) *n = s.n;
+    if (total) *total = tot;
+    if (offsets) CU(cudaMemcpy(offsets, s.offs, (s.n + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    if (codes && tot) CU(cudaMemcpy(codes, s.seq, tot, cudaMemcpyDeviceToHost));
+    return PG_OK;
+}
+
 void pg_tuning_default(pg_tuning *t)
 {
     if (!t) return;
@@ -618,6 +634,33 @@ int pg_internal_seqs(const pg_ctx *c, const uint8_t **rseq, const uint64_t **rof
 }
 
 int pg_internal_fail(int code, const char *msg) { return fail(code, "%s", msg); }
+
+// internal: the context's device and stream
+int pg_internal_device(const pg_ctx *c, int *device, void **stream)
+{
+    if (!c) return fail(PG_ERR_ARG, "null context");
+    *device = c->cfg.device;
+    *stream = (void *)c->stream;
+    return PG_OK;
+}
+
+// internal: make device arrays (cudaMalloc'd, now owned by the context) the
+// sequences of one side, as pg_set_seqs would
+int pg_internal_adopt_side(pg_ctx *c, int side, uint8_t *d_codes, uint64_t *d_offs, uint64_t n,
+                           uint32_t maxlen)
+{
+    Side &s = c->side[side];
+    if (side == 1 && c->cols_share_rows) { s = Side(); c->cols_share_rows = false; }
+    if (side == 0 && c->cols_share_rows) { c->side[1] = Side(); c->cols_share_rows = false; }
+    cudaFree(s.seq); cudaFree(s.offs);
+    s = Side();
+    s.seq = d_codes;
+    s.offs = d_offs;
+    s.n = n;
+    s.maxlen = maxlen;
+    ++c->epoch;
+    return ensure_scratch(c);
+}
 
 // internal: the context's substitution table on the device (25 x 25 int8)
 int pg_internal_score(const pg_ctx *c, const int8_t **d_sm)

@@ -199,12 +199,16 @@ def workload_features(w, device=0, mode=None):
     return feats
 
 
-def fit(w, device=0, recall=0.995, epochs=4, log=None):
-    """Label a training workload with the SW kernel, compute its features and
-    train a filter on them.  Returns (filter, threshold, metrics)."""
+def fit(w, device=0, recall=0.995, epochs=4, log=None, labels=None):
+    """Label a training workload with the SW kernel (or take the labels
+    given, e.g. whether the plain aligner's result passes the coverage/ANI
+    filter), compute its features and train a filter on them.  Returns
+    (filter, threshold, metrics)."""
     import time
     t0 = time.perf_counter()
-    _, labels = sw_labels(w, device)
+    if labels is None:
+        _, labels = sw_labels(w, device)
+    labels = np.asarray(labels, dtype=np.float32)
     t1 = time.perf_counter()
     feats = workload_features(w, device)
     f, thr, m = train(w, feats, labels, device=device, epochs=epochs, recall=recall, log=log)
