@@ -176,7 +176,10 @@ typedef struct pg_tuning {
     int32_t graph;              /* 1: pg_align / pg_align_device capture the batch's launches
                                    into a CUDA graph once per batch shape (pairs and output
                                    pointers, n, offsets, stream) and replay it after that */
-    int32_t reserved[3];
+    int32_t xd_int16;           /* 1: X-drop extension in 16-bit lanes, two cells per
+                                   instruction; an extension whose score passes 30000 is
+                                   rerun in 32 bits (needs xdrop <= 30000) */
+    int32_t reserved[2];
 } pg_tuning;                    /* 32 bytes */
 
 void pg_tuning_default(pg_tuning *t);

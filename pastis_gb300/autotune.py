@@ -2,9 +2,10 @@
 
 The choices it makes never change a result, only how fast a batch runs:
 resident blocks per SM of the DP kernels (k_ga / k_sw) and of the X-drop
-extension (k_xd), the bucketed pair order, the cap on DP rows per lane, and
-CUDA-graph replay of the batch's launches.  Candidates are timed with the
-library's own CUDA events (pg_kernel_ms) on a batch the caller supplies,
+extension (k_xd), the bucketed pair order, the cap on DP rows per lane, 16-bit
+lanes for the X-drop extension, and CUDA-graph replay of the batch's launches.
+Candidates are timed with the library's own CUDA events (pg_kernel_ms) on a
+batch the caller supplies,
 normally a sample of the real one, and the winner is cached in a JSON file
 keyed by device and a workload signature (mode, batch size and length
 quantiles, rounded to powers of two) so later runs on the same kind of batch
@@ -24,7 +25,8 @@ GRID = {
     "dp_blocks_per_sm": (1, 0),      # 0 = occupancy limit (2 on GB300)
     "xd_blocks_per_sm": (4, 0),      # 0 = occupancy limit (7 on GB300)
     "bucket_order": (1, 0),
-    "rows_max": (8, 6, 4),
+    "rows_max": (8, 6),
+    "xd_int16": (0, 1),
 }
 
 
@@ -98,7 +100,8 @@ def tune(ctx, run, key=None, device=0, reps=3, grid=None, use_cache=True, log=No
     report = {"cached": False, "key": entry, "ms": rows[0][0], "search_s": time.perf_counter() - t0,
               "candidates": len(rows), "default_ms": next(
                   (m for m, c in rows if c == {"dp_blocks_per_sm": 0, "xd_blocks_per_sm": 0,
-                                               "bucket_order": 1, "rows_max": 8, "graph": 0}),
+                                               "bucket_order": 1, "rows_max": 8, "graph": 0,
+                                               "xd_int16": 0}),
                   None)}
     if entry:
         try:

@@ -72,9 +72,11 @@ class Tuning(ctypes.Structure):
     """pg_tuning: launch shape of a context (results never depend on it)."""
     _fields_ = [("dp_blocks_per_sm", ctypes.c_int32), ("xd_blocks_per_sm", ctypes.c_int32),
                 ("bucket_order", ctypes.c_int32), ("rows_max", ctypes.c_int32),
-                ("graph", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("graph", ctypes.c_int32), ("xd_int16", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
-    FIELDS = ("dp_blocks_per_sm", "xd_blocks_per_sm", "bucket_order", "rows_max", "graph")
+    FIELDS = ("dp_blocks_per_sm", "xd_blocks_per_sm", "bucket_order", "rows_max", "graph",
+              "xd_int16")
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k in self.FIELDS}

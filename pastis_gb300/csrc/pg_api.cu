@@ -454,7 +454,8 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         if (c->tune.xd_blocks_per_sm > 0)
             xmax = std::min<uint64_t>(xmax, (uint64_t)c->nsm * (uint64_t)c->tune.xd_blocks_per_sm);
         const int gx = (int)std::min<uint64_t>(xmax, need_xd);
-        pg::k_xd<<<gx, pg::XT, 0, st>>>(kp);
+        if (c->tune.xd_int16 && c->cfg.xdrop <= pg::XMAX16) pg::k_xd16<<<gx, pg::XT, 0, st>>>(kp);
+        else pg::k_xd<<<gx, pg::XT, 0, st>>>(kp);
         pg::k_xd_wide<<<c->grid_wide, blk, 0, st>>>(kp);
         if (kp.order) {
             pg::k_hist<true><<<gsched, 256, 0, st>>>(kp);
@@ -593,6 +594,7 @@ void pg_tuning_default(pg_tuning *t)
     t->bucket_order = 1;
     t->rows_max = 8;
     t->graph = 0;
+    t->xd_int16 = 0;
 }
 
 int pg_get_tuning(const pg_ctx *c, pg_tuning *out)
@@ -612,6 +614,7 @@ int pg_set_tuning(pg_ctx *c, const pg_tuning *t)
     if (t->bucket_order != 0 && t->bucket_order != 1) return fail(PG_ERR_ARG, "bucket_order must be 0 or 1");
     if (t->rows_max < 1 || t->rows_max > 8) return fail(PG_ERR_ARG, "rows_max %d outside 1..8", t->rows_max);
     if (t->graph != 0 && t->graph != 1) return fail(PG_ERR_ARG, "graph must be 0 or 1");
+    if (t->xd_int16 != 0 && t->xd_int16 != 1) return fail(PG_ERR_ARG, "xd_int16 must be 0 or 1");
     c->tune = *t;
     std::memset(c->tune.reserved, 0, sizeof c->tune.reserved);
     ++c->epoch;                         // launch shapes changed: recapture

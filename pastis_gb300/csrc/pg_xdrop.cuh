@@ -213,4 +213,114 @@ __device__ __forceinline__ XdOut xdrop_dir_thread(const uint8_t *__restrict__ V,
     return o;
 }
 
+// ------------------------------------------------------------------------
+// The per-thread extension in 16-bit lanes, two band cells per instruction
+// (__vmaxs2 / __vaddss2 / __vcmpges2 on int16x2).  A live cell lies in
+// [best - X, best + max score], so 16 bits hold every live value while
+// best <= SAT16 and X <= XMAX16; when best passes SAT16 the routine stops and
+// reports ok = 0 (as for a band wider than the ring) and the caller reruns
+// the extension in 32 bits.  Whenever it completes its result equals
+// xdrop_dir_thread's.  Ring: 3 arrays x 8 words (16 int16 slots, column c at
+// half c & 1 of word (c >> 1) & 7), word (k, j) at wbase[(k * 8 + j) * NT].
+constexpr int UND16 = -32768;
+constexpr int SAT16 = 30000;
+constexpr int XMAX16 = 30000;
+
+template <int NT>
+__device__ __forceinline__ XdOut xdrop_dir_thread16(const uint8_t *__restrict__ V, int nv, int vstep,
+                                                    const uint8_t *__restrict__ Hs, int nh, int hstep,
+                                                    const int *__restrict__ ssm, int g, int X,
+                                                    uint32_t *__restrict__ wbase)
+{
+    XdOut o{0, 0, 0u, 1};
+    const int cols = nv + 1, rows = nh + 1;
+    if (cols == 1 || rows == 1) return o;
+#define WD(k, j) wbase[((k) * 8 + ((j) & 7)) * NT]
+#define HW(k, c) reinterpret_cast<int16_t *>(&WD(k, (c) >> 1))[(c) & 1]
+    int k1 = 0, k2 = 1, k3 = 2;
+    int off1 = 0, len1 = 0, off2 = 0, len2 = 1, off3 = 0, len3 = 2;
+    HW(k2, 0) = 0;
+    {
+        const int v1 = (-g > X) ? UND16 : g;
+        HW(k3, 0) = (int16_t)v1;
+        HW(k3, 1) = (int16_t)v1;
+    }
+    const uint32_t g2 = (uint32_t)(g & 0xffff) * 0x10001u;
+    int best = 0, d = 1, lo = 1, hi = 2;
+    while (lo < hi) {
+        ++d;
+        const int kt = k1; k1 = k2; k2 = k3; k3 = kt;
+        off1 = off2; len1 = len2;
+        off2 = off3; len2 = len3;
+        off3 = lo - 1; len3 = hi + 1 - off3;
+        if (len3 > 16 || best > SAT16) { o.ok = 0; return o; }
+        const int thr = best - X;
+        {
+            const int bval = (d * g > best - X) ? d * g : UND16;
+            HW(k3, off3) = (int16_t)((off3 == 0) ? bval : UND16);
+            HW(k3, hi) = (int16_t)((d == hi && hi < cols) ? bval : UND16);
+        }
+        const uint32_t thr2 = (uint32_t)(thr & 0xffff) * 0x10001u;
+        uint32_t db2 = 0x80008000u;
+        const int j0 = lo >> 1, j1 = (hi - 1) >> 1;
+        uint32_t a2p = WD(k2, j0 - 1), a1p = WD(k1, j0 - 1);
+        for (int j = j0; j <= j1; ++j) {
+            const int c0 = 2 * j, c1 = c0 + 1;
+            const uint32_t a2 = WD(k2, j), a1 = WD(k1, j);
+            uint32_t v = __vaddss2(__vmaxs2(__byte_perm(a2p, a2, 0x5432), a2), g2);
+            // residues V[c-1], H[d-c-1]; a half outside [lo, hi) reads a clamped
+            // index and is discarded below
+            const int vi0 = c0 - 1 > 0 ? c0 - 1 : 0;
+            const int vi1 = c1 - 1 < nv - 1 ? c1 - 1 : nv - 1;
+            const int hi0 = d - c0 - 1;
+            const int hi1 = d - c1 - 1 > 0 ? d - c1 - 1 : 0;
+            const int s0 = ssm[(int)__ldg(V + vstep * vi0) * 32 + (int)__ldg(Hs + hstep * hi0)];
+            const int s1 = ssm[(int)__ldg(V + vstep * vi1) * 32 + (int)__ldg(Hs + hstep * hi1)];
+            const uint32_t s2 = __byte_perm((uint32_t)s0, (uint32_t)s1, 0x5410);
+            v = __vmaxs2(v, __vaddss2(__byte_perm(a1p, a1, 0x5432), s2));
+            const uint32_t live = __vcmpges2(v, thr2);
+            v = (v & live) | (0x80008000u & ~live);
+            uint32_t keep = 0;
+            if (c0 < lo) keep |= 0x0000ffffu;
+            if (c1 >= hi) keep |= 0xffff0000u;
+            if (keep) v = (v & ~keep) | (WD(k3, j) & keep);
+            WD(k3, j) = v;
+            db2 = __vmaxs2(db2, v);
+            a2p = a2;
+            a1p = a1;
+        }
+        int dbest = d * g;
+        const int m0 = (int)(int16_t)(db2 & 0xffffu), m1 = (int)(int16_t)(db2 >> 16);
+        dbest = max(dbest, max(m0, m1));
+        if (dbest > best) best = dbest;
+        o.cells += (uint32_t)(hi - lo);
+        while (lo - off3 < len3 && HW(k3, lo) == UND16 && lo - off2 - 1 < len2 && HW(k2, lo - 1) == UND16)
+            ++lo;
+        while (hi - off3 > 0 && HW(k3, hi - 1) == UND16 && HW(k2, hi - 1) == UND16)
+            --hi;
+        ++hi;
+        if (lo < d + 2 - rows) lo = d + 2 - rows;
+        if (hi > cols) hi = cols;
+    }
+    int lc = off3 + len3 - 2, lr = d - lc, ls = HW(k3, lc);
+    if (ls == UND16) {
+        const int ca = off2 + len2 - 2;
+        if (HW(k2, ca) != UND16) {
+            lc = ca; lr = d - 1 - lc; ls = HW(k2, ca);
+        } else if (len2 > 2 && HW(k2, ca - 1) != UND16) {
+            lc = ca - 1; lr = d - 1 - lc; ls = HW(k2, ca - 1);
+        }
+    }
+    if (ls == UND16) {
+        for (int q = 0; q < len1; ++q) {
+            const int val = HW(k1, off1 + q);
+            if (val > ls) { ls = val; lc = off1 + q; lr = d - 2 - lc; }
+        }
+    }
+#undef HW
+#undef WD
+    if (ls != UND16) { o.dv = lc; o.dh = lr; }
+    return o;
+}
+
 }  // namespace pg

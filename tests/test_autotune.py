@@ -26,10 +26,10 @@ def test_search_picks_fastest_and_caches(native, tmp_path, monkeypatch):
     monkeypatch.setenv("PG_TUNING_CACHE", str(tmp_path / "t.json"))
     ctx = FakeCtx()
     best, rep = autotune.tune(ctx, lambda: None, key="k1", reps=2)
-    assert best == {"dp_blocks_per_sm": 0, "xd_blocks_per_sm": best["xd_blocks_per_sm"],
-                    "bucket_order": 1, "rows_max": 6, "graph": 1}
+    assert best["dp_blocks_per_sm"] == 0 and best["bucket_order"] == 1
+    assert best["rows_max"] == 6 and best["graph"] == 1
     assert ctx.t["graph"] == 1 and not rep["cached"]
-    assert rep["candidates"] == 24
+    assert rep["candidates"] == 32
     ctx2 = FakeCtx()
     best2, rep2 = autotune.tune(ctx2, lambda: None, key="k1")
     assert rep2["cached"] and best2 == best and ctx2.t["rows_max"] == 6

@@ -252,7 +252,8 @@ def test_tuning_and_graph_replay_keep_results(native, oracle_mod, mode):
     exp = O.batch(mode, codes, w.offs, codes, w.offs, w.pairs, oracle_params(O, cfg))
     kernels = 5 if mode == capi.MODE_XDROP else 3
     for t in ({}, {"bucket_order": 0}, {"rows_max": 3}, {"rows_max": 1, "dp_blocks_per_sm": 1},
-              {"xd_blocks_per_sm": 2}, {"graph": 1}, {"graph": 1, "bucket_order": 0}):
+              {"xd_blocks_per_sm": 2}, {"graph": 1}, {"graph": 1, "bucket_order": 0},
+              {"xd_int16": 1}, {"xd_int16": 1, "graph": 1}):
         ctx.set_tuning(capi.default_tuning(), **t)
         for rep in range(2):                 # the second call replays the graph
             got = ctx.align(w.pairs)
@@ -275,4 +276,35 @@ def test_tuning_and_graph_replay_keep_results(native, oracle_mod, mode):
         ctx.set_tuning(rows_max=9)
     with pytest.raises(capi.PgError):
         ctx.set_tuning(graph=2)
+    ctx.close()
+
+
+def test_int16_extension_saturation_reruns_in_32_bits(native, oracle_mod):
+    """Pairs of identical 3500-residue sequences rich in W and C push the
+    X-drop score past the 16-bit lanes' limit (30000): those extensions are
+    rerun in 32 bits and every result still equals the oracle's."""
+    from pastis_gb300 import capi
+    rng = np.random.default_rng(17)
+    letters = np.frombuffer(b"WCWCWYHW", dtype=np.uint8)
+    seqs = [letters[rng.integers(0, len(letters), 3500)] for _ in range(3)]
+    seqs.append(np.frombuffer(b"ACDEFGHIKLMNPQRSTVWY" * 20, dtype=np.uint8))
+    ascii_ = np.concatenate(seqs)
+    offs = np.cumsum([0] + [len(x) for x in seqs]).astype(np.uint64)
+    pairs = np.zeros(4, dtype=capi.PAIR_DTYPE)
+    pairs["row"] = [0, 1, 2, 3]
+    pairs["col"] = [0, 1, 2, 3]
+    pairs["rs0"] = pairs["cs0"] = [1700, 10, 3000, 50]
+    pairs["rs1"] = pairs["cs1"] = [100, 3400, 3000, 300]
+    pairs["count"] = 2
+    cfg = capi.config(capi.MODE_XDROP)
+    ctx = capi.Context(cfg)
+    ctx.set_seqs(0, ascii_, offs)
+    ctx.share_row_seqs()
+    ctx.set_tuning(xd_int16=1)
+    got = ctx.align(pairs)
+    O = oracle_mod
+    codes = O.encode(bytes(ascii_))
+    exp = O.batch(capi.MODE_XDROP, codes, offs, codes, offs, pairs, oracle_params(O, cfg))
+    assert_same(got, exp, pairs)
+    assert got["score"][0] > 30000
     ctx.close()
