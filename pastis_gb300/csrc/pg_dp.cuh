@@ -13,10 +13,13 @@
 //   F(i,j) = max(F(i-1,j) + ext, H(i-1,j) + first)      vertical gap
 //   H(i,j) = max(H(i-1,j-1) + s, F, E [, 0])
 // Inside a lane only F runs down the rows.  The lane carries A = F + ext and
-// G = H + first, so the chain from one row to the next is two DPX operations:
-//   F = vibmax(G_up, A_up)        G = viaddmax(F, first, max(diag, E) + first)
-// while the diagonal, E and every statistic select depend only on the previous
-// column and sit off that chain.  The DPX predicates give the winner of each
+// G = H + first, so the chain from one row to the next is
+//   F = vibmax(G_up, A_up)        H = max(X, F)        G = H + first
+// with X = max(diag, E); the diagonal, E and every statistic select depend
+// only on the previous column and sit off that chain.  (G as
+// viaddmax(F, first, X + first) gives a two-op chain but one instruction more
+// per cell; with the ALU pipe the bound, the shorter issue count measured
+// 1-2 % faster.)  The DPX predicates give the winner of each
 // maximum; statistics (pg_stats.cuh) follow the predecessor a traceback would
 // choose under the tie policy TIE, so the end cell carries the statistics of
 // the traced alignment.  A gap opened from a cell whose best path already ends
@@ -238,10 +241,10 @@ __device__ DpOut<S> dp_warp(const uint8_t *__restrict__ V, int m,
                     int F;
                     if (OPEN_FIRST) { F = __vibmax_s32(cG, cA, &pf); }
                     else { bool px; F = __vibmax_s32(cA, cG, &px); pf = !px; }
-                    const int G = __viaddmax_s32(F, go, X + go);
                     const int A = F + ge;
                     // ---- H and its statistics
                     const int Hv = max(X, F);
+                    const int G = Hv + go;
                     const bool chF = E_FIRST ? (F > X) : (F > dg && F >= E);
                     const S SF = S::sel(pf, cSHoF, cSF);
                     S SH = S::sel(chF, SF, SX);
