@@ -195,6 +195,9 @@ __device__ DpOut<S> dp_warp(const uint8_t *__restrict__ V, int m,
         // residue of the column this lane works on next (prefetched one step ahead)
         int hc_next = (lane == 0) ? (int)__ldg(Hs) : 0;
 
+        // this lane's first maximum in this row block: score, j << 3 | row, statistics
+        int sbs = 0, sbp = 0;
+        S sbst = S::zero();
         const int nsteps = n + t_last;
         for (int k = 0; k < nsteps; ++k) {
             const Edge<S> rcv = out.shfl_up();
@@ -211,6 +214,7 @@ __device__ DpOut<S> dp_warp(const uint8_t *__restrict__ V, int m,
             const int hc = hc_next;
             hc_next = (j >= 0 && j < n) ? (int)__ldg(Hs + j) : 0;
             if (lane_on && j >= 1 && j <= n) {
+                const int j8 = j << 3;
                 const uint2 pw = prof[hc * 32 + lane];
                 int cG = in.h + go, cA = in.a, cH = in.h;
                 S cSF = in.sf, cSHoF = in.shof, cSH = in.sh;
@@ -265,11 +269,12 @@ __device__ DpOut<S> dp_warp(const uint8_t *__restrict__ V, int m,
                     SEl[r] = SE; SHoEl[r] = SHoE; SHl[r] = SH;
                     cG = G; cA = A; cH = Hv; cSF = SF; cSHoF = SHoF; cSH = SH;
                     if (S::LOCAL) {
-                        // first maximum in column-major order; within a lane a
-                        // later row block can only win a tie by a smaller column
-                        if (valid[r] && (Hv > bs || (Hv == bs && Hv > 0 && j < bj))) {
-                            bs = Hv; bi = rb + lane * R + r + 1; bj = j; bst = SH;
-                        }
+                        // a lane meets its cells of one row block in column-major
+                        // order, so the first maximum is a strict improvement
+                        const bool take = valid[r] && Hv > sbs;
+                        sbs = take ? Hv : sbs;
+                        sbp = take ? j8 + r : sbp;
+                        sbst = S::sel(take, SH, sbst);
                     }
                 }
                 out.h = cH; out.a = cA; out.sf = cSF; out.shof = cSHoF; out.sh = cSH;
@@ -277,6 +282,14 @@ __device__ DpOut<S> dp_warp(const uint8_t *__restrict__ V, int m,
             }
         }
         __syncwarp();
+        if (S::LOCAL && sbs > 0) {
+            // first maximum in column-major order: against earlier row blocks
+            // (smaller rows) a tie goes to the smaller column only
+            const int sj = sbp >> 3;
+            if (sbs > bs || (sbs == bs && sj < bj)) {
+                bs = sbs; bj = sj; bi = rb + lane * R + (sbp & 7) + 1; bst = sbst;
+            }
+        }
         if (!S::LOCAL && last_block) {
             // H(m, n) lives in lane t_last, row (rows_here - 1) % R
             const int rl = (rows_here - 1) % R;

@@ -1,6 +1,6 @@
 // pg_kernels.cuh -- batch kernels behind pg_align (sm_103a).
 //
-// --sxa (X-drop), three launches per batch:
+// --sxa (X-drop), five launches per batch:
 //   k_xd       one thread per (pair, seed): both X-drop directions on a
 //              16-slot per-thread ring in shared memory (the band of the
 //              default gap model never spans more than 13 columns); threads
@@ -8,11 +8,14 @@
 //              short extensions balance.  Writes the extended region.
 //   k_xd_wide  one warp per (pair, seed) whose band outgrew the thread ring:
 //              256-slot shared ring, per-warp global ring beyond that.
+//              (k_xd16, the 16-bit-lane form of k_xd, is a tuning option.)
+//   k_hist, k_bucket  the bucket order of the pairs for k_ga (schedule below).
 //   k_ga       one warp per pair: global alignment with statistics over each
 //              seed's region (a region equal to the first seed's is not
 //              realigned: an equal identity never replaces the kept one),
 //              best identity, coverage/ANI filter, result record.
-// --sfa (SW): k_sw, one warp per pair, local alignment with statistics.
+// --sfa (SW): k_hist, k_bucket, then k_sw, one warp per pair, local
+// alignment with statistics.
 //
 // All kernels are persistent with work stealing (grids sized to the resident
 // capacity) so pairs of very different lengths balance themselves.
