@@ -350,7 +350,8 @@ def run_gpu(args, rank, world, local_rank):
             "executed_cells_split": {"extension": exec_xd, "alignment": exec_dp},
             "roofline": {"bound": "dpx", "achieved": achieved, "peak": peak_gcups,
                          "unit": "GCUPS", "frac": achieved / peak_gcups, "traffic": traffic,
-                         "kernel": "k_ga" if mode else "k_sw",
+                         "kernel": ("k_ga_dir + k_tb_ga" if mode else "k_sw_dir + k_tb_sw")
+                         if ctx.get_tuning().dp_traceback else ("k_ga" if mode else "k_sw"),
                          "kernel_ms": dp_ms, "kernel_cells": exec_dp,
                          "peak_source": "measured %.4g DPX add-max/s (pg_dpx_peak) / %d "
                                         "int32 DPX ops per cell" % (peak_ops, DPX_OPS_PER_CELL),
@@ -396,8 +397,12 @@ def tuned_arm(args, w, ctx, mode, dev, stream, flush, d_pairs, plain_res, plain_
     def run_sample():
         ctx.align_device(d_pairs.data_ptr(), ns, d_out.data_ptr(), stream.cuda_stream)
 
+    def run_full():
+        ctx.align_device(d_pairs.data_ptr(), n, d_out.data_ptr(), stream.cuda_stream)
+
     key = autotune.signature(mode, w.pairs, w.lengths())
-    best, rep = autotune.tune(ctx, run_sample, key=key, device=dev, use_cache=False)
+    best, rep = autotune.tune(ctx, run_sample, key=key, device=dev, use_cache=False,
+                              validate=run_full if ns < n else None)
     for _ in range(max(args.warmup, 3)):
         ctx.align_device(d_pairs.data_ptr(), n, d_out.data_ptr(), stream.cuda_stream)
     torch.cuda.synchronize(dev)
@@ -417,7 +422,8 @@ def tuned_arm(args, w, ctx, mode, dev, stream, flush, d_pairs, plain_res, plain_
             "results_identical_to_plain": bool(same),
             "search": {"sample_pairs": ns, "candidates": rep.get("candidates"),
                        "seconds": rep.get("search_s"), "best_sample_ms": rep.get("ms"),
-                       "default_sample_ms": rep.get("default_ms"), "key": key}}
+                       "default_sample_ms": rep.get("default_ms"), "key": key,
+                       "full_batch_check": rep.get("validated_on_full_batch")}}
 
 
 def filtered_arm(args, w, ctx, dev, stream, flush, d_pairs, plain_res, plain_ms):

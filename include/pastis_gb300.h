@@ -179,9 +179,15 @@ typedef struct pg_tuning {
     int32_t xd_int16;           /* 1: X-drop extension in 16-bit lanes, two cells per
                                    instruction; an extension whose score passes 30000 is
                                    rerun in 32 bits (needs xdrop <= 30000) */
-    int32_t reserved[2];
+    int32_t dp_traceback;       /* 1: the alignment DP stores a 4-bit decision per cell in an
+                                   HBM arena (up to a third of the device memory, in chunks
+                                   beyond that) and a traceback pass counts the statistics;
+                                   no graph capture in this form */
+    int32_t dir_arena_mb;       /* cap on that arena in MiB; 0 = a third of the device memory */
 } pg_tuning;                    /* 32 bytes */
 
+/* The built-in tuning; a new context starts from it, with dp_traceback on for
+ * PG_MODE_SW (measured faster there, slower for the X-drop global alignment). */
 void pg_tuning_default(pg_tuning *t);
 int  pg_get_tuning(const pg_ctx *ctx, pg_tuning *out);
 /* PG_ERR_ARG on a value out of range. */

@@ -2,8 +2,9 @@
 
 The choices it makes never change a result, only how fast a batch runs:
 resident blocks per SM of the DP kernels (k_ga / k_sw) and of the X-drop
-extension (k_xd), the bucketed pair order, the cap on DP rows per lane, 16-bit
-lanes for the X-drop extension, and CUDA-graph replay of the batch's launches.
+extension (k_xd), the bucketed pair order, 16-bit lanes for the X-drop
+extension, the traceback form of the alignment DP, and CUDA-graph replay of
+the batch's launches.
 Candidates are timed with the library's own CUDA events (pg_kernel_ms) on a
 batch the caller supplies,
 normally a sample of the real one, and the winner is cached in a JSON file
@@ -25,8 +26,8 @@ GRID = {
     "dp_blocks_per_sm": (1, 0),      # 0 = occupancy limit (2 on GB300)
     "xd_blocks_per_sm": (4, 0),      # 0 = occupancy limit (7 on GB300)
     "bucket_order": (1, 0),
-    "rows_max": (8, 6),
     "xd_int16": (0, 1),
+    "dp_traceback": (0, 1),
 }
 
 
@@ -69,9 +70,13 @@ def _time(ctx, run, reps):
     return statistics.median(ms)
 
 
-def tune(ctx, run, key=None, device=0, reps=3, grid=None, use_cache=True, log=None):
+def tune(ctx, run, key=None, device=0, reps=3, grid=None, use_cache=True, log=None,
+         validate=None):
     """Time every candidate tuning with `run()` (one batch on ctx) and set the
-    fastest on ctx, with graph replay on.  Returns (tuning dict, report)."""
+    fastest on ctx, with graph replay on.  With `validate` (a run of the full
+    batch) the winner is timed against the context's tuning before the search
+    and kept only if faster: a sample can mislead when a few long pairs dominate it.
+    Returns (tuning dict, report)."""
     path = cache_path()
     dev = _device_name(device)
     entry = "%s|%s" % (dev, key) if key else None
@@ -83,6 +88,7 @@ def tune(ctx, run, key=None, device=0, reps=3, grid=None, use_cache=True, log=No
         if cached:
             ctx.set_tuning(capi.default_tuning(), **cached["tuning"])
             return cached["tuning"], {"cached": True, "key": entry, "ms": cached.get("ms")}
+    initial = ctx.get_tuning().as_dict() if validate is not None else None
     grid = GRID if grid is None else grid
     names = list(grid)
     rows = []
@@ -96,12 +102,22 @@ def tune(ctx, run, key=None, device=0, reps=3, grid=None, use_cache=True, log=No
             log("%-70s %.3f ms" % (cand, ms))
     rows.sort(key=lambda r: r[0])
     best = dict(rows[0][1], graph=1)
+    validated = None
+    if validate is not None:
+        base = dict(initial)
+        ctx.set_tuning(capi.default_tuning(), **best)
+        t_best = _time(ctx, validate, 2)
+        ctx.set_tuning(capi.default_tuning(), **base)
+        t_base = _time(ctx, validate, 2)
+        validated = {"best_ms": t_best, "default_ms": t_base}
+        if t_base < t_best:
+            best = base
     ctx.set_tuning(capi.default_tuning(), **best)
     report = {"cached": False, "key": entry, "ms": rows[0][0], "search_s": time.perf_counter() - t0,
-              "candidates": len(rows), "default_ms": next(
+              "candidates": len(rows), "validated_on_full_batch": validated, "default_ms": next(
                   (m for m, c in rows if c == {"dp_blocks_per_sm": 0, "xd_blocks_per_sm": 0,
-                                               "bucket_order": 1, "rows_max": 8, "graph": 0,
-                                               "xd_int16": 0}),
+                                               "bucket_order": 1, "graph": 0,
+                                               "xd_int16": 0, "dp_traceback": 0}),
                   None)}
     if entry:
         try:

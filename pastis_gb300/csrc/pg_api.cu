@@ -12,7 +12,10 @@
 #include <new>
 
 #include "../../include/pastis_gb300.h"
+#include <cub/device/device_scan.cuh>
+
 #include "pg_kernels.cuh"
+#include "pg_kernels_dir.cuh"
 
 namespace {
 
@@ -132,6 +135,15 @@ struct pg_ctx {
     uint64_t xd_cap = 0;
     uint32_t *d_order = nullptr;        // bucket order of the pairs
     uint64_t order_cap = 0;
+    // traceback form: direction arena, per-task byte counts / offsets,
+    // per-pair scores and end cells, scan scratch
+    uint8_t *d_dir = nullptr;
+    uint64_t dir_cap = 0, dir_budget = 0;
+    uint64_t *d_dbytes = nullptr, *d_doff = nullptr, *d_t1 = nullptr;
+    int *d_dsc = nullptr;
+    void *d_scan = nullptr;
+    size_t scan_bytes = 0;
+    uint64_t dirb_cap = 0;
     // staging for the host-buffer entry point
     pg_pair *d_pairs = nullptr;
     pg_result *d_out = nullptr;
@@ -216,6 +228,8 @@ void pg_destroy(pg_ctx *ctx)
     cudaFree(ctx->d_xd);
     cudaFree(ctx->d_ovf);
     cudaFree(ctx->d_order);
+    cudaFree(ctx->d_dir); cudaFree(ctx->d_dbytes); cudaFree(ctx->d_doff); cudaFree(ctx->d_t1);
+    cudaFree(ctx->d_dsc); cudaFree(ctx->d_scan);
     cudaFree(ctx->d_pairs);
     cudaFree(ctx->d_out);
     for (int k = 0; k < 3; ++k)
@@ -282,6 +296,20 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     CUD(cudaFuncSetAttribute(pg::k_sw<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
     CUD(cudaFuncSetAttribute(pg::k_sw<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
     CUD(cudaFuncSetAttribute(pg::k_sw<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_ga_dir<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_ga_dir<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_ga_dir<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_ga_dir<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_sw_dir<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_sw_dir<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_sw_dir<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(cudaFuncSetAttribute(pg::k_sw_dir<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    {
+        // the direction arena may take up to a third of the device memory
+        size_t fr = 0, tot = 0;
+        CUD(cudaMemGetInfo(&fr, &tot));
+        c->dir_budget = std::max<uint64_t>((uint64_t)1 << 30, (uint64_t)tot / 3);
+    }
     int per_sm = 0;
     if (cfg->mode == PG_MODE_XDROP) {
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pg::k_ga<0>, pg::WARPS * 32, pg::DP_DYN_SMEM));
@@ -297,6 +325,9 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     c->dp_per_sm = std::max(per_sm, 1);
     c->xd_per_sm = c->grid_xd ? c->grid_xd / c->nsm : 1;
     pg_tuning_default(&c->tune);
+    // local alignment in the traceback form measured 1.47x faster (sw100k:
+    // 24.7 -> 16.8 ms); the X-drop global alignment is faster with statistics
+    if (cfg->mode == PG_MODE_SW) c->tune.dp_traceback = 1;
 #undef CUD
     *out = c;
     return PG_OK;
@@ -413,6 +444,98 @@ int pg_share_row_seqs(pg_ctx *c)
     return ensure_scratch(c);
 }
 
+// The traceback form of the DP phase: direction bytes per task, their
+// offsets, then per chunk of consecutive tasks whose matrices fit the arena
+// the DP kernel and the traceback kernel.  Reads the total size back to the
+// host (one synchronization per batch, one more per extra chunk).
+static int run_dir(pg_ctx *c, const pg::KParams &kp, uint64_t n, int grid, cudaStream_t st)
+{
+    const bool xdrop = c->cfg.mode == PG_MODE_XDROP;
+    if (n + 1 > c->dirb_cap) {
+        cudaFree(c->d_dbytes); cudaFree(c->d_doff); cudaFree(c->d_dsc); cudaFree(c->d_t1);
+        cudaFree(c->d_scan);
+        c->d_dbytes = nullptr; c->d_doff = nullptr; c->d_dsc = nullptr; c->d_t1 = nullptr;
+        c->d_scan = nullptr; c->dirb_cap = 0; c->scan_bytes = 0;
+        CU(cudaMalloc(&c->d_dbytes, (n + 1) * sizeof(uint64_t)));
+        CU(cudaMalloc(&c->d_doff, (n + 1) * sizeof(uint64_t)));
+        CU(cudaMalloc(&c->d_dsc, n * 4 * sizeof(int)));
+        CU(cudaMalloc(&c->d_t1, sizeof(uint64_t)));
+        CU(cub::DeviceScan::ExclusiveSum(nullptr, c->scan_bytes, c->d_dbytes, c->d_doff, n + 1));
+        CU(cudaMalloc(&c->d_scan, c->scan_bytes));
+        c->dirb_cap = n + 1;
+    }
+    const int gs = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (n + 256) / 256);
+    if (xdrop) pg::k_dirsize<true><<<gs, 256, 0, st>>>(kp, c->d_dbytes);
+    else pg::k_dirsize<false><<<gs, 256, 0, st>>>(kp, c->d_dbytes);
+    size_t sb = c->scan_bytes;
+    CU(cub::DeviceScan::ExclusiveSum(c->d_scan, sb, c->d_dbytes, c->d_doff, n + 1, st));
+    uint64_t total = 0;
+    CU(cudaMemcpyAsync(&total, c->d_doff + n, sizeof total, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    const uint64_t budget = c->tune.dir_arena_mb > 0 ? ((uint64_t)c->tune.dir_arena_mb << 20) : c->dir_budget;
+    if (c->dir_cap > budget) {           // a smaller cap than the arena held so far
+        cudaFree(c->d_dir);
+        c->d_dir = nullptr; c->dir_cap = 0;
+    }
+    const uint64_t want = std::max<uint64_t>(16, std::min<uint64_t>(total, budget));
+    if (want > c->dir_cap) {
+        cudaFree(c->d_dir);
+        c->d_dir = nullptr; c->dir_cap = 0;
+        CU(cudaMalloc(&c->d_dir, want));
+        c->dir_cap = want;
+    }
+    const dim3 blk(pg::WARPS * 32);
+    const int dyn = pg::DP_DYN_SMEM;
+    const int tie = c->cfg.tie;
+    int launches = 1;
+    uint64_t t0 = 0;
+    while (t0 < n) {
+        uint64_t t1 = n;
+        if (total > c->dir_cap) {
+            pg::k_chunk_end<<<1, 32, 0, st>>>(c->d_doff, t0, n, c->dir_cap, c->d_t1);
+            uint64_t lim[3] = {0, 0, 0};
+            CU(cudaMemcpyAsync(&lim[0], c->d_t1, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+            CU(cudaStreamSynchronize(st));
+            t1 = lim[0];
+            CU(cudaMemcpyAsync(&lim[1], c->d_doff + t0, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+            CU(cudaMemcpyAsync(&lim[2], c->d_doff + t1, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+            CU(cudaStreamSynchronize(st));
+            if (lim[2] - lim[1] > c->dir_cap) {          // one task larger than the arena
+                cudaFree(c->d_dir);
+                c->d_dir = nullptr; c->dir_cap = 0;
+                CU(cudaMalloc(&c->d_dir, lim[2] - lim[1]));
+                c->dir_cap = lim[2] - lim[1];
+            }
+            launches += 1;
+        }
+        CU(cudaMemsetAsync(c->d_counter + 3, 0, sizeof(unsigned int), st));
+        const uint64_t nt = t1 - t0;
+        const int g = (int)std::min<uint64_t>((uint64_t)grid, (nt + pg::WARPS - 1) / pg::WARPS);
+        const int gt = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (nt + 255) / 256);
+        if (xdrop) {
+            switch (tie) {
+            case 0: pg::k_ga_dir<0><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
+            case 1: pg::k_ga_dir<1><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
+            case 2: pg::k_ga_dir<2><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
+            default: pg::k_ga_dir<3><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
+            }
+            pg::k_tb_ga<<<gt, 256, 0, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc);
+        } else {
+            switch (tie) {
+            case 0: pg::k_sw_dir<0><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
+            case 1: pg::k_sw_dir<1><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
+            case 2: pg::k_sw_dir<2><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
+            default: pg::k_sw_dir<3><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
+            }
+            pg::k_tb_sw<<<gt, 256, 0, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc);
+        }
+        CU(cudaGetLastError());
+        launches += 2;
+        t0 = t1;
+    }
+    return launches;   // k_dirsize, then per chunk (k_chunk_end,) the DP and the traceback
+}
+
 static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, uint64_t coff,
                   pg_result *d_out, cudaStream_t st)
 {
@@ -438,6 +561,7 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
     kp.sched = c->d_counter + 4;
     kp.order = c->tune.bucket_order ? c->d_order : nullptr;
     kp.rows_cap = c->tune.rows_max;
+    kp.dir = c->tune.dp_traceback;
     CU(cudaMemsetAsync(c->d_counter, 0, (4 + pg::SCHED_WORDS) * sizeof(unsigned int), st));
     CU(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
     const uint64_t need_blocks = (n + pg::WARPS - 1) / pg::WARPS;
@@ -463,13 +587,19 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         }
         CU(cudaEventRecord(c->ev[1], st));
         const int dyn = pg::DP_DYN_SMEM;
-        switch (c->cfg.tie) {
-        case 0: pg::k_ga<0><<<grid, blk, dyn, st>>>(kp); break;
-        case 1: pg::k_ga<1><<<grid, blk, dyn, st>>>(kp); break;
-        case 2: pg::k_ga<2><<<grid, blk, dyn, st>>>(kp); break;
-        default: pg::k_ga<3><<<grid, blk, dyn, st>>>(kp); break;
+        if (kp.dir) {
+            const int l = run_dir(c, kp, n, (int)gmax, st);
+            if (l < 0) return l;
+            c->last_launches = (kp.order ? 4 : 2) + l;
+        } else {
+            switch (c->cfg.tie) {
+            case 0: pg::k_ga<0><<<grid, blk, dyn, st>>>(kp); break;
+            case 1: pg::k_ga<1><<<grid, blk, dyn, st>>>(kp); break;
+            case 2: pg::k_ga<2><<<grid, blk, dyn, st>>>(kp); break;
+            default: pg::k_ga<3><<<grid, blk, dyn, st>>>(kp); break;
+            }
+            c->last_launches = kp.order ? 5 : 3;
         }
-        c->last_launches = kp.order ? 5 : 3;
     } else {
         if (kp.order) {
             pg::k_hist<false><<<gsched, 256, 0, st>>>(kp);
@@ -477,13 +607,19 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         }
         CU(cudaEventRecord(c->ev[1], st));
         const int dyn = pg::DP_DYN_SMEM;
-        switch (c->cfg.tie) {
-        case 0: pg::k_sw<0><<<grid, blk, dyn, st>>>(kp); break;
-        case 1: pg::k_sw<1><<<grid, blk, dyn, st>>>(kp); break;
-        case 2: pg::k_sw<2><<<grid, blk, dyn, st>>>(kp); break;
-        default: pg::k_sw<3><<<grid, blk, dyn, st>>>(kp); break;
+        if (kp.dir) {
+            const int l = run_dir(c, kp, n, (int)gmax, st);
+            if (l < 0) return l;
+            c->last_launches = (kp.order ? 2 : 0) + l;
+        } else {
+            switch (c->cfg.tie) {
+            case 0: pg::k_sw<0><<<grid, blk, dyn, st>>>(kp); break;
+            case 1: pg::k_sw<1><<<grid, blk, dyn, st>>>(kp); break;
+            case 2: pg::k_sw<2><<<grid, blk, dyn, st>>>(kp); break;
+            default: pg::k_sw<3><<<grid, blk, dyn, st>>>(kp); break;
+            }
+            c->last_launches = kp.order ? 3 : 1;
         }
-        c->last_launches = kp.order ? 3 : 1;
     }
     CU(cudaEventRecord(c->ev[2], st));
     c->events_valid = true;
@@ -495,7 +631,9 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
 static int enqueue(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, uint64_t coff,
                    pg_result *d_out, cudaStream_t st)
 {
-    if (!c->tune.graph || n == 0) return launch(c, d_pairs, n, roff, coff, d_out, st);
+    // the traceback form reads sizes back to the host mid-batch: no capture
+    if (!c->tune.graph || c->tune.dp_traceback || n == 0)
+        return launch(c, d_pairs, n, roff, coff, d_out, st);
     if (!c->side[0].seq || !c->side[1].seq) return fail(PG_ERR_STATE, "sequences not set");
     int rc = ensure_batch(c, n);       // every allocation happens outside the capture
     if (rc) return rc;
@@ -595,6 +733,8 @@ void pg_tuning_default(pg_tuning *t)
     t->rows_max = 8;
     t->graph = 0;
     t->xd_int16 = 0;
+    t->dp_traceback = 0;
+    t->dir_arena_mb = 0;
 }
 
 int pg_get_tuning(const pg_ctx *c, pg_tuning *out)
@@ -615,8 +755,9 @@ int pg_set_tuning(pg_ctx *c, const pg_tuning *t)
     if (t->rows_max < 1 || t->rows_max > 8) return fail(PG_ERR_ARG, "rows_max %d outside 1..8", t->rows_max);
     if (t->graph != 0 && t->graph != 1) return fail(PG_ERR_ARG, "graph must be 0 or 1");
     if (t->xd_int16 != 0 && t->xd_int16 != 1) return fail(PG_ERR_ARG, "xd_int16 must be 0 or 1");
+    if (t->dp_traceback != 0 && t->dp_traceback != 1) return fail(PG_ERR_ARG, "dp_traceback must be 0 or 1");
+    if (t->dir_arena_mb < 0) return fail(PG_ERR_ARG, "dir_arena_mb must be >= 0");
     c->tune = *t;
-    std::memset(c->tune.reserved, 0, sizeof c->tune.reserved);
     ++c->epoch;                         // launch shapes changed: recapture
     return PG_OK;
 }

@@ -199,6 +199,10 @@ __device__ DpOut<S> dp_warp(const uint8_t *__restrict__ V, int m,
         int sbs = 0, sbp = 0;
         S sbst = S::zero();
         const int nsteps = n + t_last;
+        // Two columns per trip for the local form lets the compiler alternate
+        // register sets instead of copying the carried values (sw100k 352 ->
+        // 376 GCUPS); the global form measured 15 % slower that way.
+#pragma unroll (S::LOCAL ? 2 : 1)
         for (int k = 0; k < nsteps; ++k) {
             const Edge<S> rcv = out.shfl_up();
             const int dgH = in.h;

@@ -72,6 +72,7 @@ struct KParams {
     unsigned int *sched = nullptr;   // [0, NBUCKET) bucket sizes, [NBUCKET, 2*NBUCKET) cursors
     const uint32_t *order = nullptr; // pair taken as the t-th task by k_ga / k_sw (null: t)
     int rows_cap = 8;                // cap on DP rows per lane (tuning)
+    int dir = 0;                     // 1: the traceback form (pg_kernels_dir.cuh) runs the DP
 };
 
 __device__ __forceinline__ void load_sm(int *ssm, const int8_t *sm)
@@ -392,12 +393,15 @@ __device__ __forceinline__ int pair_bucket(const KParams &kp, uint64_t p)
         m = r.ev - r.bv;
         n = r.eh - r.bh;
         if (m <= 0 || n <= 0) return BUCKET_NONE;
+        // the traceback form has no statistics words: one family up to 8 rows
+        if (kp.dir) return 12 - dp_rows_per_lane<S1>(m, kp.rows_cap);                             // 4..11
         if (m > S1::MAXSIDE || n > S1::MAXSIDE) return 4 - dp_rows_per_lane<S2>(m, kp.rows_cap);   // 0..3
         return 12 - dp_rows_per_lane<S1>(m, kp.rows_cap);                                           // 4..11
     }
     const pg_pair pr = kp.pairs[p];
     const uint8_t *V, *Hs;
     if (!pair_seqs(kp, pr, V, m, Hs, n) || m == 0 || n == 0) return BUCKET_NONE;
+    if (kp.dir) return 12 - dp_rows_per_lane<S1>(m, kp.rows_cap);                                  // 4..11
     if (m > L1::MAXSIDE || n > L1::MAXSIDE) return 4 - dp_rows_per_lane<L2>(m, kp.rows_cap);        // 0..3
     return 8 - dp_rows_per_lane<L1>(m, kp.rows_cap);                                                // 4..7
 }

@@ -1,0 +1,304 @@
+// pg_kernels_dir.cuh -- the traceback form of the alignment kernels (tuning
+// option dp_traceback): k_ga_dir / k_sw_dir run dp_warp_dir (one warp per
+// pair, direction nibbles into an HBM arena), k_tb_ga / k_tb_sw trace them
+// back (one thread per pair) and write the same pg_result records k_ga /
+// k_sw write.  A batch whose direction matrices exceed the arena runs in
+// chunks of consecutive tasks (bucket order), each chunk DP then traceback.
+#pragma once
+#include <cstdint>
+
+#include "pg_dpdir.cuh"
+#include "pg_kernels.cuh"
+#include "pg_trace.cuh"
+
+namespace pg {
+
+// rows per lane of the traceback DP: no statistics registers, so up to 8
+__device__ __forceinline__ int dir_rows(int m, int cap) { return dp_rows_per_lane<S1>(m, cap); }
+
+// which seeds of an X-drop pair get a DP of their own, with their regions
+// (the choices of k_ga: not tried, same seed, same region, empty region)
+struct SeedPlan {
+    XdRec rec[2];
+    bool dp[2];
+};
+
+__device__ __forceinline__ SeedPlan seed_plan(const KParams &kp, uint64_t p)
+{
+    SeedPlan sp;
+    sp.rec[0] = kp.xd[2 * p];
+    sp.rec[1] = kp.xd[2 * p + 1];
+    const XdRec &a = sp.rec[0], &b = sp.rec[1];
+    sp.dp[0] = !(a.flags & (XF_NONE | XF_BADIDX)) && a.ev > a.bv && a.eh > a.bh;
+    const bool same_region = !(a.flags & XF_NONE) && b.bv == a.bv && b.ev == a.ev &&
+                             b.bh == a.bh && b.eh == a.eh;
+    sp.dp[1] = !(b.flags & (XF_NONE | XF_SAME | XF_BADIDX)) && !same_region && b.ev > b.bv &&
+               b.eh > b.bh;
+    return sp;
+}
+
+__device__ __forceinline__ uint64_t region_dir_bytes(const XdRec &r, int cap)
+{
+    const int m = r.ev - r.bv, n = r.eh - r.bh;
+    return dir_bytes(m, n, dir_rows(m, cap));
+}
+
+// direction bytes of each task (bucket position t)
+template <bool XDROP>
+__global__ void k_dirsize(const KParams kp, uint64_t *bytes)
+{
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t <= kp.n;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        if (t == kp.n) { bytes[t] = 0; continue; }
+        const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
+        uint64_t b = 0;
+        if (p < kp.n) {
+            if (XDROP) {
+                const SeedPlan sp = seed_plan(kp, p);
+                if (sp.dp[0]) b += region_dir_bytes(sp.rec[0], kp.rows_cap);
+                if (sp.dp[1]) b += region_dir_bytes(sp.rec[1], kp.rows_cap);
+            } else {
+                const pg_pair pr = kp.pairs[p];
+                const uint8_t *V, *Hs;
+                int m, n;
+                if (pair_seqs(kp, pr, V, m, Hs, n)) b = dir_bytes(m, n, dir_rows(m, kp.rows_cap));
+            }
+        }
+        bytes[t] = b;
+    }
+}
+
+// end of the chunk that starts at task t0: the largest t1 <= n with
+// doff[t1] - doff[t0] <= budget, at least t0 + 1
+__global__ void k_chunk_end(const uint64_t *doff, uint64_t t0, uint64_t n, uint64_t budget,
+                            uint64_t *t1)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const uint64_t base = doff[t0];
+    uint64_t lo = t0 + 1, hi = n;   // answer in [lo, hi]
+    if (doff[lo] - base > budget) { *t1 = lo; return; }
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi + 1) >> 1;
+        if (doff[mid] - base <= budget) lo = mid; else hi = mid - 1;
+    }
+    *t1 = lo;
+}
+
+template <int TIE, bool LOCAL>
+__device__ __forceinline__ DirOut dp_dispatch_dir(const uint8_t *V, int m, const uint8_t *Hs, int n,
+                                                  const int *ssm, uint2 *prof, int go, int ge,
+                                                  void *bnd, uint32_t *dir, int cap)
+{
+    EdgeD *b = (EdgeD *)bnd;
+    switch (dir_rows(m, cap)) {
+    case 1: return dp_warp_dir<TIE, 1, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+    case 2: return dp_warp_dir<TIE, 2, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+    case 3: return dp_warp_dir<TIE, 3, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+    case 4: return dp_warp_dir<TIE, 4, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+    case 5: return dp_warp_dir<TIE, 5, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+    case 6: return dp_warp_dir<TIE, 6, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+    case 7: return dp_warp_dir<TIE, 7, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+    default: return dp_warp_dir<TIE, 8, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+    }
+}
+
+// ---------------------------------------------------------------- X-drop
+// DP of each seed region of the tasks [t0, t1); a task's regions sit at
+// arena + doff[t] - doff[t0] (seed 0 first).  dsc[2p + s] = global score.
+template <int TIE>
+__global__ void __launch_bounds__(WARPS * 32, 2) k_ga_dir(const KParams kp, uint64_t t0, uint64_t t1,
+                                                         const uint64_t *doff, uint8_t *arena, int *dsc)
+{
+    __shared__ int ssm[32 * 32];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
+    const uint64_t gw = (uint64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    void *bnd = (char *)kp.bnd + gw * kp.bnd_bytes;
+    uint2 *prof = g_dyn_prof + (threadIdx.x >> 5) * (NCODES * 32);
+    const int lane = threadIdx.x & 31;
+    unsigned long long exec = 0;
+    const uint64_t base = doff[t0];
+    WarpQueue q;
+    uint64_t u;
+    while (q.pop(&kp.counter[3], t1 - t0, u)) {
+        const uint64_t t = t0 + u;
+        const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
+        if (p >= kp.n) continue;
+        const pg_pair pr = kp.pairs[p];
+        const uint8_t *V, *Hs;
+        int m, n;
+        if (!pair_seqs(kp, pr, V, m, Hs, n)) continue;
+        const SeedPlan sp = seed_plan(kp, p);
+        uint64_t off = doff[t] - base;
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            if (!sp.dp[s]) continue;
+            const XdRec &r = sp.rec[s];
+            const int rm = r.ev - r.bv, rn = r.eh - r.bh;
+            const DirOut d = dp_dispatch_dir<TIE, false>(V + r.bv, rm, Hs + r.bh, rn, ssm, prof, kp.go,
+                                                         kp.ge, bnd, (uint32_t *)(arena + off),
+                                                         kp.rows_cap);
+            if (lane == 0) dsc[2 * p + s] = d.score;
+            exec += (uint64_t)rm * (uint64_t)rn;
+            off += dir_bytes(rm, rn, dir_rows(rm, kp.rows_cap));
+        }
+    }
+    if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
+}
+
+// traceback and result of the tasks [t0, t1), one thread per task: the same
+// record k_ga writes
+__global__ void __launch_bounds__(256) k_tb_ga(const KParams kp, uint64_t t0, uint64_t t1,
+                                               const uint64_t *doff, const uint8_t *arena,
+                                               const int *dsc)
+{
+    const uint64_t base = doff[t0];
+    const int gmax = kp.go > kp.ge ? kp.go : kp.ge;
+    for (uint64_t t = t0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < t1;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
+        if (p >= kp.n) { atomicOr(kp.status, ST_BAD_SCHED); continue; }
+        const pg_pair pr = kp.pairs[p];
+        const uint8_t *V, *Hs;
+        int m, n;
+        pg_result best = empty_result();
+        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
+            atomicOr(kp.status, ST_BAD_INDEX);
+            kp.out[p] = best;
+            continue;
+        }
+        const SeedPlan sp = seed_plan(kp, p);
+        uint64_t off = doff[t] - base;
+        uint64_t cells = 0;
+        bool have = false, bad = false;
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const XdRec &rec = sp.rec[s];
+            if (rec.flags & XF_NONE) continue;
+            if (rec.flags & XF_SAME) {
+                const XdRec &r0 = sp.rec[0];
+                cells += (uint64_t)r0.cells + (uint64_t)(r0.ev - r0.bv) * (uint64_t)(r0.eh - r0.bh);
+                continue;
+            }
+            if (rec.flags & XF_BAD) bad = true;
+            const int bv = rec.bv, ev = rec.ev, bh = rec.bh, eh = rec.eh;
+            const int rm = ev - bv, rn = eh - bh;
+            cells += rec.cells + (uint64_t)rm * (uint64_t)rn;
+            const bool same_region = s == 1 && !(sp.rec[0].flags & XF_NONE) && bv == sp.rec[0].bv &&
+                                     ev == sp.rec[0].ev && bh == sp.rec[0].bh && eh == sp.rec[0].eh;
+            if (same_region) continue;
+            int score;
+            uint32_t M = 0, D = 0, G = 0;
+            if (rm > 0 && rn > 0) {
+                score = dsc[2 * p + s];
+                const int R = dir_rows(rm, kp.rows_cap);
+                const TraceOut tr = trace_back<false>((const uint32_t *)(arena + off), rn, R, rm, rn,
+                                                      V + bv, Hs + bh);
+                M = tr.M; D = tr.D; G = tr.G;
+                off += dir_bytes(rm, rn, R);
+            } else if (rm + rn > 0) {
+                score = kp.go + (rm + rn - 1) * gmax;   // one gap run
+                G = 1;
+            } else {
+                score = 0;
+            }
+            const uint32_t L = (uint32_t)(rm + rn) - D;
+            pg_result cur;
+            cur.score = score; cur.aln_len = L; cur.matches = M; cur.gap_opens = G;
+            cur.beg_v = (uint16_t)bv; cur.end_v = (uint16_t)ev;
+            cur.beg_h = (uint16_t)bh; cur.end_h = (uint16_t)eh;
+            cur.seed_used = (uint8_t)s; cur.pad = 0; cur.cells = 0; cur.score_aln = 0.0f;
+            if (L == 0) { cur.identity = 0.0f; cur.flags = PG_RF_EMPTY; }
+            else { cur.identity = identity_of(M, L); cur.flags = 0; }
+            const bool cur_nan = (cur.flags & PG_RF_EMPTY) != 0;
+            const bool best_nan = (best.flags & PG_RF_EMPTY) != 0;
+            if (!have || (!cur_nan && !best_nan && cur.identity > best.identity)) {
+                best = cur;
+                have = true;
+            }
+        }
+        best.cells = sat_u32(cells);
+        if (bad) best.flags |= PG_RF_BAD_SEED;
+        apply_filter(best, m, n, kp.cov_thr, kp.ani_thr);
+        kp.out[p] = best;
+    }
+}
+
+// ---------------------------------------------------------------- SW
+// local DP of the tasks [t0, t1); dsc[4p ..] = score, end row, end column, have
+template <int TIE>
+__global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint64_t t0, uint64_t t1,
+                                                      const uint64_t *doff, uint8_t *arena, int *dsc)
+{
+    __shared__ int ssm[32 * 32];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
+    const uint64_t gw = (uint64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    void *bnd = (char *)kp.bnd + gw * kp.bnd_bytes;
+    uint2 *prof = g_dyn_prof + (threadIdx.x >> 5) * (NCODES * 32);
+    const int lane = threadIdx.x & 31;
+    unsigned long long exec = 0;
+    const uint64_t base = doff[t0];
+    WarpQueue q;
+    uint64_t u;
+    while (q.pop(&kp.counter[3], t1 - t0, u)) {
+        const uint64_t t = t0 + u;
+        const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
+        if (p >= kp.n) continue;
+        const pg_pair pr = kp.pairs[p];
+        const uint8_t *V, *Hs;
+        int m, n;
+        if (!pair_seqs(kp, pr, V, m, Hs, n)) continue;
+        exec += (unsigned long long)m * (unsigned long long)n;
+        DirOut d;
+        d.score = 0; d.ei = 0; d.ej = 0; d.have = 0;
+        if (m > 0 && n > 0)
+            d = dp_dispatch_dir<TIE, true>(V, m, Hs, n, ssm, prof, kp.go, kp.ge, bnd,
+                                           (uint32_t *)(arena + (doff[t] - base)), kp.rows_cap);
+        if (lane == 0) {
+            int4 *o = reinterpret_cast<int4 *>(dsc) + p;
+            *o = make_int4(d.score, d.ei, d.ej, d.have);
+        }
+    }
+    if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
+}
+
+// traceback and result of the tasks [t0, t1), one thread per task: the same
+// record k_sw writes
+__global__ void __launch_bounds__(256) k_tb_sw(const KParams kp, uint64_t t0, uint64_t t1,
+                                               const uint64_t *doff, const uint8_t *arena,
+                                               const int *dsc)
+{
+    const uint64_t base = doff[t0];
+    for (uint64_t t = t0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < t1;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
+        if (p >= kp.n) { atomicOr(kp.status, ST_BAD_SCHED); continue; }
+        const pg_pair pr = kp.pairs[p];
+        const uint8_t *V, *Hs;
+        int m, n;
+        pg_result o = empty_result();
+        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
+            atomicOr(kp.status, ST_BAD_INDEX);
+            kp.out[p] = o;
+            continue;
+        }
+        o.cells = sat_u32((uint64_t)m * (uint64_t)n);
+        const int4 d = reinterpret_cast<const int4 *>(dsc)[p];
+        if (m > 0 && n > 0 && d.w) {
+            const int R = dir_rows(m, kp.rows_cap);
+            const TraceOut tr = trace_back<true>((const uint32_t *)(arena + (doff[t] - base)), n, R,
+                                                 d.y, d.z, V, Hs);
+            const uint32_t L = (uint32_t)((d.y - tr.i0) + (d.z - tr.j0)) - tr.D;
+            o.score = d.x;
+            o.aln_len = L; o.matches = tr.M; o.gap_opens = tr.G;
+            o.beg_v = (uint16_t)tr.i0; o.end_v = (uint16_t)d.y;
+            o.beg_h = (uint16_t)tr.j0; o.end_h = (uint16_t)d.z;
+            if (L > 0) { o.identity = identity_of(tr.M, L); o.flags = 0; }
+        }
+        apply_filter(o, m, n, kp.cov_thr, kp.ani_thr);
+        kp.out[p] = o;
+    }
+}
+
+}  // namespace pg

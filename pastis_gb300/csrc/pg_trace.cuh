@@ -1,0 +1,76 @@
+// pg_trace.cuh -- traceback over the direction nibbles of dp_warp_dir
+// (pg_dpdir.cuh): one thread walks one region from its end cell back to its
+// start and counts what computeAlignmentStats counts
+// (src/align/SeqanFullAligner.cpp:238-246): diagonal columns, identical
+// columns, and gap runs (maximal runs of same-orientation gap moves).
+//
+// The walk follows the DP's own decisions, so its path is the one whose
+// statistics dp_warp carries to the end cell: H-state cells move as their
+// source says (diagonal, or into the F / E gap state of the same cell), a gap
+// state moves one row up (F) or one column left (E) and returns to H-state
+// when its gap was opened.  Borders: a global alignment reaching row 0 or
+// column 0 finishes along it in one gap run; a local alignment stops there,
+// or at a cell whose H fell to 0, and starts at that cell.
+#pragma once
+#include <cstdint>
+
+#include "pg_dpdir.cuh"
+
+namespace pg {
+
+struct TraceOut {
+    uint32_t M, D, G;
+    int i0, j0;
+};
+
+template <bool LOCAL>
+__device__ TraceOut trace_back(const uint32_t *__restrict__ dir, int n, int R, int i, int j,
+                               const uint8_t *__restrict__ V, const uint8_t *__restrict__ Hs)
+{
+    uint32_t M = 0, D = 0, G = 0;
+    int state = 0;   // 0: H, 1: F (vertical gap), 2: E (horizontal gap)
+    int last = 0;    // orientation of the previous move: 0 diagonal / none, 1 vertical, 2 horizontal
+    const int rows = 32 * R;
+    for (;;) {
+        if (i == 0 || j == 0) {
+            if (!LOCAL) {
+                if (i > 0 && last != 1) ++G;
+                else if (j > 0 && last != 2) ++G;
+            }
+            break;
+        }
+        const int r0 = i - 1;
+        const int stripe = r0 / rows, within = r0 - stripe * rows;
+        const int lane = within / R, r = within - lane * R;
+        const uint32_t w = __ldg(dir + ((uint64_t)stripe * (uint64_t)n + (uint64_t)(j - 1)) * 32u + lane);
+        const uint32_t nib = (w >> (4 * r)) & 15u;
+        if (state == 0) {
+            const uint32_t hs = nib & 3u;
+            if (hs == DIR_ZERO) break;
+            if (hs == DIR_DIAG) {
+                ++D;
+                M += __ldg(V + i - 1) == __ldg(Hs + j - 1) ? 1u : 0u;
+                --i; --j;
+                last = 0;
+                continue;
+            }
+            state = hs == DIR_F ? 1 : 2;
+        }
+        if (state == 1) {
+            if (last != 1) ++G;
+            last = 1;
+            state = (nib & DIR_FOPEN) ? 0 : 1;
+            --i;
+        } else {
+            if (last != 2) ++G;
+            last = 2;
+            state = (nib & DIR_EOPEN) ? 0 : 2;
+            --j;
+        }
+    }
+    TraceOut o;
+    o.M = M; o.D = D; o.G = G; o.i0 = i; o.j0 = j;
+    return o;
+}
+
+}  // namespace pg

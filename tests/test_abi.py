@@ -49,7 +49,8 @@ def test_tuning_defaults_without_gpu(native):
     from pastis_gb300 import capi
     t = capi.default_tuning()
     assert t.as_dict() == {"dp_blocks_per_sm": 0, "xd_blocks_per_sm": 0, "bucket_order": 1,
-                           "rows_max": 8, "graph": 0, "xd_int16": 0}
+                           "rows_max": 8, "graph": 0, "xd_int16": 0, "dp_traceback": 0,
+                           "dir_arena_mb": 0}
 
 
 def test_defaults_and_errors_without_gpu(native):

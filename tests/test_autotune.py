@@ -16,7 +16,7 @@ class FakeCtx:
 
     def kernel_ms(self):
         t = self.t
-        ms = 10.0 + (2.0 if t["bucket_order"] == 0 else 0.0) + abs(t["rows_max"] - 6) * 0.5
+        ms = 10.0 + (2.0 if t["bucket_order"] == 0 else 0.0) + (0.5 if t["dp_traceback"] else 0.0)
         ms += 1.0 if t["dp_blocks_per_sm"] == 1 else 0.0
         return 0.0, ms
 
@@ -27,12 +27,12 @@ def test_search_picks_fastest_and_caches(native, tmp_path, monkeypatch):
     ctx = FakeCtx()
     best, rep = autotune.tune(ctx, lambda: None, key="k1", reps=2)
     assert best["dp_blocks_per_sm"] == 0 and best["bucket_order"] == 1
-    assert best["rows_max"] == 6 and best["graph"] == 1
+    assert best["graph"] == 1
     assert ctx.t["graph"] == 1 and not rep["cached"]
     assert rep["candidates"] == 32
     ctx2 = FakeCtx()
     best2, rep2 = autotune.tune(ctx2, lambda: None, key="k1")
-    assert rep2["cached"] and best2 == best and ctx2.t["rows_max"] == 6
+    assert rep2["cached"] and best2 == best and ctx2.t["dp_traceback"] == 0
 
 
 def test_signature_rounds_to_powers_of_two(native):

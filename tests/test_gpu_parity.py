@@ -43,7 +43,9 @@ def run_both(mode, w, cfg, O, pairs=None, roff=0, coff=0, share=True):
     else:
         ctx.set_seqs(1, ascii_, w.offs)
     got = ctx.align(pairs, roff, coff)
-    assert ctx.last_launches() == (5 if mode == capi.MODE_XDROP else 3)
+    # X-drop: k_xd, k_xd_wide, k_hist, k_bucket, k_ga; SW (traceback form):
+    # k_hist, k_bucket, k_dirsize, k_sw_dir, k_tb_sw
+    assert ctx.last_launches() == 5
     codes = O.encode(bytes(ascii_))
     exp = O.batch(mode, codes, w.offs, codes, w.offs, pairs, oracle_params(O, cfg),
                   bl_roff=roff, bl_coff=coff)
@@ -253,13 +255,16 @@ def test_tuning_and_graph_replay_keep_results(native, oracle_mod, mode):
     kernels = 5 if mode == capi.MODE_XDROP else 3
     for t in ({}, {"bucket_order": 0}, {"rows_max": 3}, {"rows_max": 1, "dp_blocks_per_sm": 1},
               {"xd_blocks_per_sm": 2}, {"graph": 1}, {"graph": 1, "bucket_order": 0},
-              {"xd_int16": 1}, {"xd_int16": 1, "graph": 1}):
+              {"xd_int16": 1}, {"xd_int16": 1, "graph": 1}, {"dp_traceback": 1},
+              {"dp_traceback": 1, "dir_arena_mb": 1}, {"dp_traceback": 1, "rows_max": 3},
+              {"dp_traceback": 1, "bucket_order": 0, "graph": 1}):
         ctx.set_tuning(capi.default_tuning(), **t)
         for rep in range(2):                 # the second call replays the graph
             got = ctx.align(w.pairs)
             assert_same(got, exp, w.pairs)
         want = kernels if t.get("bucket_order", 1) else kernels - 2
-        assert ctx.last_launches() == want, t
+        if not t.get("dp_traceback"):
+            assert ctx.last_launches() == want, t
     # device entry point with graph replay on a caller stream
     n = len(w.pairs)
     d_pairs = torch.from_numpy(w.pairs.view(np.uint8).copy()).cuda()
@@ -308,3 +313,44 @@ def test_int16_extension_saturation_reruns_in_32_bits(native, oracle_mod):
     assert_same(got, exp, pairs)
     assert got["score"][0] > 30000
     ctx.close()
+
+
+@pytest.mark.parametrize("tie", [0, 1, 2, 3])
+@pytest.mark.parametrize("gaps", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_traceback_form_parity(sw_small, xd_small, oracle_mod, tie, gaps, mode):
+    """The traceback form of the DP (direction nibbles in HBM, then a walk
+    back) gives the oracle's results under every tie policy and gap model."""
+    from pastis_gb300 import capi
+    w = sw_small if mode == capi.MODE_SW else xd_small
+    cfg = capi.config(mode, tie=tie, gap_semantics=gaps)
+    ctx = capi.Context(cfg)
+    ctx.set_seqs(0, w.ascii, w.offs)
+    ctx.share_row_seqs()
+    ctx.set_tuning(dp_traceback=1)
+    got = ctx.align(w.pairs)
+    O = oracle_mod
+    codes = O.encode(bytes(w.ascii))
+    exp = O.batch(mode, codes, w.offs, codes, w.offs, w.pairs, oracle_params(O, cfg))
+    assert_same(got, exp, w.pairs)
+    ctx.close()
+
+
+def test_traceback_form_long_regions(native, oracle_mod):
+    """Regions over 1023 rows and columns (several stripes of 256 rows, the
+    wide-statistics case of the other form), both modes, small arena chunks."""
+    from pastis_gb300 import capi, synth
+    w = synth.generate("uneven10m", seed=5, scale=0.00003)
+    O = oracle_mod
+    codes = O.encode(bytes(w.ascii))
+    for mode in (capi.MODE_SW, capi.MODE_XDROP):
+        cfg = capi.config(mode)
+        ctx = capi.Context(cfg)
+        ctx.set_seqs(0, w.ascii, w.offs)
+        ctx.share_row_seqs()
+        ctx.set_tuning(dp_traceback=1, dir_arena_mb=2)
+        got = ctx.align(w.pairs)
+        exp = O.batch(mode, codes, w.offs, codes, w.offs, w.pairs, oracle_params(O, cfg))
+        assert_same(got, exp, w.pairs)
+        ctx.close()
+
