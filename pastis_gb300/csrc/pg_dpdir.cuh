@@ -14,9 +14,13 @@
 //             after this cell)
 //   bit 2     E(i, j) was opened from H(i, j-1) (else extended from E(i, j-1))
 //   bit 3     F(i, j) was opened from H(i-1, j) (else extended from F(i-1, j))
-// Layout of one region: word ((stripe * n) + j - 1) * 32 + lane holds the
-// nibbles of the lane's R rows (row r of the lane in bits 4r..4r+3) at
-// column j, so a warp writes 128 contiguous bytes per column step.
+// Layout of one region: the nibbles of a lane's R rows at column j (row r of
+// the lane in bits 4r..4r+3) sit in word (stripe * (n + 31) + k) * 32 + lane,
+// k = j - 1 + lane the wavefront step that computes them, so every store of
+// a warp fills 128 contiguous bytes (a [column][lane] layout scatters one
+// step's 32 words over 32 lines: measured 2x the DRAM writes plus
+// write-allocate reads), and a traceback moving left or up walks back through
+// neighbouring lines.
 #pragma once
 #include <cstdint>
 
@@ -62,7 +66,7 @@ __host__ __device__ __forceinline__ uint64_t dir_bytes(int m, int n, int R)
 {
     if (m <= 0 || n <= 0) return 0;
     const uint64_t stripes = (uint64_t)((m + 32 * R - 1) / (32 * R));
-    return stripes * (uint64_t)n * 128ull;
+    return stripes * (uint64_t)(n + 31) * 128ull;
 }
 
 struct DirOut {
@@ -121,7 +125,7 @@ __device__ DirOut dp_warp_dir(const uint8_t *__restrict__ V, int m,
         EdgeD in = dir_col0<LOCAL>(i_up, go, ge, gmax);
         EdgeD out = dir_col0<LOCAL>(i_bot, go, ge, gmax);
         int hc_next = (lane == 0) ? (int)__ldg(Hs) : 0;
-        uint32_t *dcol = dir + (uint64_t)stripe * (uint64_t)n * 32u + lane;
+        uint32_t *dstep = dir + (uint64_t)stripe * (uint64_t)(n + 31) * 32u + lane;
         int sbs = 0, sbp = 0;
         const int nsteps = n + t_last;
         for (int k = 0; k < nsteps; ++k) {
@@ -174,7 +178,7 @@ __device__ DirOut dp_warp_dir(const uint8_t *__restrict__ V, int m,
                         sbp = take ? (j << 3) + r : sbp;
                     }
                 }
-                dcol[(uint64_t)(j - 1) * 32u] = word;
+                dstep[(uint64_t)k * 32u] = word;
                 out.h = cH; out.a = cA;
                 if (!last_block && lane == t_last) bnd[j] = out;
             }

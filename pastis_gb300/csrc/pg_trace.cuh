@@ -42,7 +42,8 @@ __device__ TraceOut trace_back(const uint32_t *__restrict__ dir, int n, int R, i
         const int r0 = i - 1;
         const int stripe = r0 / rows, within = r0 - stripe * rows;
         const int lane = within / R, r = within - lane * R;
-        const uint32_t w = __ldg(dir + ((uint64_t)stripe * (uint64_t)n + (uint64_t)(j - 1)) * 32u + lane);
+        const uint32_t w = __ldg(dir + ((uint64_t)stripe * (uint64_t)(n + 31) +
+                                        (uint64_t)(j - 1 + lane)) * 32u + lane);
         const uint32_t nib = (w >> (4 * r)) & 15u;
         if (state == 0) {
             const uint32_t hs = nib & 3u;
