@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="CPU work per baseline sample (seconds)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--set-tuning", default="",
+                    help="launch tuning of the plain arm, e.g. dp_traceback=0,bucket_order=1")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuned arm (tuned)")
     ap.add_argument("--no-filter", action="store_true",
@@ -220,6 +222,9 @@ def run_gpu(args, rank, world, local_rank):
     ctx = capi.Context(cfg)
     ctx.set_seqs(0, w.ascii, w.offs)
     ctx.share_row_seqs()
+    if args.set_tuning:
+        ctx.set_tuning(**{k: int(v) for k, v in
+                          (kv.split("=") for kv in args.set_tuning.split(","))})
 
     # a dedicated stream: the kernels and the timing events must share it
     stream = torch.cuda.Stream(device=dev)
@@ -310,10 +315,13 @@ def run_gpu(args, rank, world, local_rank):
         # dominant kernel: the alignment DP (k_ga / k_sw), its own cells and time
         achieved = exec_dp / (dp_ms * 1e-3) / 1e9
         traffic = None
+        dp_kernel = (("k_ga_dir + k_tb_ga" if mode else "k_sw_dir + k_tb_sw")
+                     if ctx.get_tuning().dp_traceback else ("k_ga" if mode else "k_sw"))
         tpath = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tpath):
+            # ncu DRAM bytes per pair of the same kernel on this workload
             tr = json.load(open(tpath)).get(args.workload)
-            if tr and tr.get("bytes_per_pair"):
+            if tr and tr.get("bytes_per_pair") and tr.get("kernel") == dp_kernel:
                 traffic = tr["bytes_per_pair"] * n
         peaks = {}
         ppath = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -350,8 +358,7 @@ def run_gpu(args, rank, world, local_rank):
             "executed_cells_split": {"extension": exec_xd, "alignment": exec_dp},
             "roofline": {"bound": "dpx", "achieved": achieved, "peak": peak_gcups,
                          "unit": "GCUPS", "frac": achieved / peak_gcups, "traffic": traffic,
-                         "kernel": ("k_ga_dir + k_tb_ga" if mode else "k_sw_dir + k_tb_sw")
-                         if ctx.get_tuning().dp_traceback else ("k_ga" if mode else "k_sw"),
+                         "kernel": dp_kernel,
                          "kernel_ms": dp_ms, "kernel_cells": exec_dp,
                          "peak_source": "measured %.4g DPX add-max/s (pg_dpx_peak) / %d "
                                         "int32 DPX ops per cell" % (peak_ops, DPX_OPS_PER_CELL),

@@ -168,6 +168,7 @@ struct pg_ctx {
         }
     } gkey{};
     int graph_launches = 0;
+    bool capturing = false;             // launch() is being recorded into a graph
 };
 
 extern "C" {
@@ -536,6 +537,15 @@ static int run_dir(pg_ctx *c, const pg::KParams &kp, uint64_t n, int grid, cudaS
     return launches;   // k_dirsize, then per chunk (k_chunk_end,) the DP and the traceback
 }
 
+// The batch timing events.  Inside a stream capture they become external
+// event-record nodes, so the host can still wait on them after a replay (a
+// plain record node leaves an event the host cannot synchronize on).
+static cudaError_t record_event(const pg_ctx *c, cudaEvent_t e, cudaStream_t st)
+{
+    return c->capturing ? cudaEventRecordWithFlags(e, st, cudaEventRecordExternal)
+                        : cudaEventRecord(e, st);
+}
+
 static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, uint64_t coff,
                   pg_result *d_out, cudaStream_t st)
 {
@@ -571,7 +581,7 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
     const int grid = (int)std::min<uint64_t>(gmax, need_blocks);
     const dim3 blk(pg::WARPS * 32);
     const int gsched = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (n + 255) / 256);
-    CU(cudaEventRecord(c->ev[0], st));
+    CU(record_event(c, c->ev[0], st));
     if (c->cfg.mode == PG_MODE_XDROP) {
         const uint64_t need_xd = (2 * n + pg::XT - 1) / pg::XT;
         uint64_t xmax = (uint64_t)c->grid_xd;
@@ -585,7 +595,7 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
             pg::k_hist<true><<<gsched, 256, 0, st>>>(kp);
             pg::k_bucket<true><<<gsched, 256, 0, st>>>(kp);
         }
-        CU(cudaEventRecord(c->ev[1], st));
+        CU(record_event(c, c->ev[1], st));
         const int dyn = pg::DP_DYN_SMEM;
         if (kp.dir) {
             const int l = run_dir(c, kp, n, (int)gmax, st);
@@ -605,7 +615,7 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
             pg::k_hist<false><<<gsched, 256, 0, st>>>(kp);
             pg::k_bucket<false><<<gsched, 256, 0, st>>>(kp);
         }
-        CU(cudaEventRecord(c->ev[1], st));
+        CU(record_event(c, c->ev[1], st));
         const int dyn = pg::DP_DYN_SMEM;
         if (kp.dir) {
             const int l = run_dir(c, kp, n, (int)gmax, st);
@@ -621,7 +631,7 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
             c->last_launches = kp.order ? 3 : 1;
         }
     }
-    CU(cudaEventRecord(c->ev[2], st));
+    CU(record_event(c, c->ev[2], st));
     c->events_valid = true;
     CU(cudaGetLastError());
     return PG_OK;
@@ -641,7 +651,9 @@ static int enqueue(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff,
     if (!c->gexec || !(key == c->gkey)) {
         if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
         CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        c->capturing = true;
         rc = launch(c, d_pairs, n, roff, coff, d_out, st);
+        c->capturing = false;
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(st, &g);
         if (rc) { if (g) cudaGraphDestroy(g); return rc; }

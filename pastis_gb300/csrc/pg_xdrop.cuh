@@ -272,7 +272,8 @@ __device__ __forceinline__ XdOut xdrop_dir_thread16(const uint8_t *__restrict__ 
             // index and is discarded below
             const int vi0 = c0 - 1 > 0 ? c0 - 1 : 0;
             const int vi1 = c1 - 1 < nv - 1 ? c1 - 1 : nv - 1;
-            const int hi0 = d - c0 - 1;
+            // (a discarded low half c0 = lo - 1 can ask for H[nh], one past the end)
+            const int hi0 = d - c0 - 1 < nh - 1 ? d - c0 - 1 : nh - 1;
             const int hi1 = d - c1 - 1 > 0 ? d - c1 - 1 : 0;
             const int s0 = ssm[(int)__ldg(V + vstep * vi0) * 32 + (int)__ldg(Hs + hstep * hi0)];
             const int s1 = ssm[(int)__ldg(V + vstep * vi1) * 32 + (int)__ldg(Hs + hstep * hi1)];

@@ -262,6 +262,8 @@ def test_tuning_and_graph_replay_keep_results(native, oracle_mod, mode):
         for rep in range(2):                 # the second call replays the graph
             got = ctx.align(w.pairs)
             assert_same(got, exp, w.pairs)
+            ext_ms, aln_ms = ctx.kernel_ms()     # the timing events survive a replay
+            assert ext_ms >= 0 and aln_ms > 0, t
         want = kernels if t.get("bucket_order", 1) else kernels - 2
         if not t.get("dp_traceback"):
             assert ctx.last_launches() == want, t
