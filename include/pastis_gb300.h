@@ -182,7 +182,10 @@ typedef struct pg_tuning {
     int32_t dp_traceback;       /* 1: the alignment DP stores a 4-bit decision per cell in an
                                    HBM arena (up to a third of the device memory, in chunks
                                    beyond that) and a traceback pass counts the statistics;
-                                   no graph capture in this form */
+                                   2: the same, with two cells per instruction on 16-bit
+                                   lanes for every region whose scores provably fit 16 bits
+                                   ((m + n + 4) * largest |score| <= 30000), 32-bit lanes for
+                                   the rest; no graph capture in either form */
     int32_t dir_arena_mb;       /* cap on that arena in MiB; 0 = a third of the device memory */
 } pg_tuning;                    /* 32 bytes */
 

@@ -19,13 +19,13 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC]
-CUDA_UNITS = ("pg_api.cu", "pg_filter.cu", "pg_kmer.cu", "pg_fasta.cu")
+CUDA_UNITS = ("pg_api.cu", "pg_stat.cu", "pg_dir.cu", "pg_filter.cu", "pg_kmer.cu", "pg_fasta.cu")
 
 
 def _steps():
     """Build steps in dependency order; each step is a list of independent
     jobs (output name, command without -o, dependencies) run in parallel."""
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers += [os.path.join(INC, "pastis_gb300.h")]
     objs = []
     compile_jobs = []

@@ -14,8 +14,10 @@
 #include "../../include/pastis_gb300.h"
 #include <cub/device/device_scan.cuh>
 
+#include "pg_dir.h"
+#include "pg_stat.h"
 #include "pg_kernels.cuh"
-#include "pg_kernels_dir.cuh"
+#include "pg_kernels_xd.cuh"
 
 namespace {
 
@@ -155,6 +157,7 @@ struct pg_ctx {
     // launch tuning and the captured graph of the last batch shape
     pg_tuning tune{};
     int dp_per_sm = 1, xd_per_sm = 1;   // occupancy limits
+    int lim16 = 0;                      // largest m + n for 16-bit lanes (dp_traceback 2)
     uint64_t epoch = 0;                 // bumped whenever a buffer a graph holds moves
     cudaGraphExec_t gexec = nullptr;
     struct GraphKey {
@@ -277,6 +280,12 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     } else {
         c->go = cfg->gap_open; c->ge = cfg->gap_ext; c->xg = cfg->gap_ext;
     }
+    {
+        // regions that the traceback form may run on 16-bit lanes
+        int maxabs = std::max(std::abs(c->go), std::abs(c->ge));
+        for (int k = 0; k < PG_NRES * PG_NRES; ++k) maxabs = std::max(maxabs, std::abs((int)c->sm[k]));
+        c->lim16 = pg::dir16_limit(maxabs);
+    }
 #define CUD(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { pg_destroy(c); \
         return fail(e_ == cudaErrorMemoryAllocation ? PG_ERR_OOM : PG_ERR_CUDA, "%s: %s", #call, \
                     cudaGetErrorString(e_)); } } while (0)
@@ -289,22 +298,8 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     CUD(cudaMemset(c->d_exec, 0, 2 * sizeof(unsigned long long)));
     for (int k = 0; k < 3; ++k) CUD(cudaEventCreate(&c->ev[k]));
     CUD(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, cfg->device));
-    CUD(cudaFuncSetAttribute(pg::k_ga<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_ga<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_ga<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_ga<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_sw<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_sw<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_sw<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_sw<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_ga_dir<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_ga_dir<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_ga_dir<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_ga_dir<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_sw_dir<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_sw_dir<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_sw_dir<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
-    CUD(cudaFuncSetAttribute(pg::k_sw_dir<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::DP_DYN_SMEM));
+    CUD(pg::stat_set_attributes());
+    CUD(pg::dir_set_attributes());
     {
         // the direction arena may take up to a third of the device memory
         size_t fr = 0, tot = 0;
@@ -313,14 +308,14 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     }
     int per_sm = 0;
     if (cfg->mode == PG_MODE_XDROP) {
-        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pg::k_ga<0>, pg::WARPS * 32, pg::DP_DYN_SMEM));
+        CUD(pg::stat_occupancy(true, &per_sm));
         int px = 0, pw = 0;
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&px, pg::k_xd, pg::XT, 0));
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pw, pg::k_xd_wide, pg::WARPS * 32, 0));
         c->grid_xd = c->nsm * std::max(px, 1);
         c->grid_wide = c->nsm * std::max(pw, 1);
     } else {
-        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pg::k_sw<0>, pg::WARPS * 32, pg::DP_DYN_SMEM));
+        CUD(pg::stat_occupancy(false, &per_sm));
     }
     c->grid = c->nsm * std::max(per_sm, 1);
     c->dp_per_sm = std::max(per_sm, 1);
@@ -466,8 +461,7 @@ static int run_dir(pg_ctx *c, const pg::KParams &kp, uint64_t n, int grid, cudaS
         c->dirb_cap = n + 1;
     }
     const int gs = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (n + 256) / 256);
-    if (xdrop) pg::k_dirsize<true><<<gs, 256, 0, st>>>(kp, c->d_dbytes);
-    else pg::k_dirsize<false><<<gs, 256, 0, st>>>(kp, c->d_dbytes);
+    pg::dir_sizes(xdrop, kp, c->d_dbytes, gs, st);
     size_t sb = c->scan_bytes;
     CU(cub::DeviceScan::ExclusiveSum(c->d_scan, sb, c->d_dbytes, c->d_doff, n + 1, st));
     uint64_t total = 0;
@@ -485,15 +479,14 @@ static int run_dir(pg_ctx *c, const pg::KParams &kp, uint64_t n, int grid, cudaS
         CU(cudaMalloc(&c->d_dir, want));
         c->dir_cap = want;
     }
-    const dim3 blk(pg::WARPS * 32);
-    const int dyn = pg::DP_DYN_SMEM;
+    const int dyn = kp.dir16_lim > 0 ? pg::DIR16_DYN_SMEM : pg::DP_DYN_SMEM;
     const int tie = c->cfg.tie;
     int launches = 1;
     uint64_t t0 = 0;
     while (t0 < n) {
         uint64_t t1 = n;
         if (total > c->dir_cap) {
-            pg::k_chunk_end<<<1, 32, 0, st>>>(c->d_doff, t0, n, c->dir_cap, c->d_t1);
+            pg::dir_chunk_end(c->d_doff, t0, n, c->dir_cap, c->d_t1, st);
             uint64_t lim[3] = {0, 0, 0};
             CU(cudaMemcpyAsync(&lim[0], c->d_t1, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
             CU(cudaStreamSynchronize(st));
@@ -513,23 +506,7 @@ static int run_dir(pg_ctx *c, const pg::KParams &kp, uint64_t n, int grid, cudaS
         const uint64_t nt = t1 - t0;
         const int g = (int)std::min<uint64_t>((uint64_t)grid, (nt + pg::WARPS - 1) / pg::WARPS);
         const int gt = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (nt + 255) / 256);
-        if (xdrop) {
-            switch (tie) {
-            case 0: pg::k_ga_dir<0><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
-            case 1: pg::k_ga_dir<1><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
-            case 2: pg::k_ga_dir<2><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
-            default: pg::k_ga_dir<3><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
-            }
-            pg::k_tb_ga<<<gt, 256, 0, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc);
-        } else {
-            switch (tie) {
-            case 0: pg::k_sw_dir<0><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
-            case 1: pg::k_sw_dir<1><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
-            case 2: pg::k_sw_dir<2><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
-            default: pg::k_sw_dir<3><<<g, blk, dyn, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc); break;
-            }
-            pg::k_tb_sw<<<gt, 256, 0, st>>>(kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc);
-        }
+        pg::dir_run(xdrop, tie, kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc, g, dyn, gt, st);
         CU(cudaGetLastError());
         launches += 2;
         t0 = t1;
@@ -571,7 +548,8 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
     kp.sched = c->d_counter + 4;
     kp.order = c->tune.bucket_order ? c->d_order : nullptr;
     kp.rows_cap = c->tune.rows_max;
-    kp.dir = c->tune.dp_traceback;
+    kp.dir = c->tune.dp_traceback ? 1 : 0;
+    kp.dir16_lim = c->tune.dp_traceback == 2 ? c->lim16 : 0;
     CU(cudaMemsetAsync(c->d_counter, 0, (4 + pg::SCHED_WORDS) * sizeof(unsigned int), st));
     CU(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
     const uint64_t need_blocks = (n + pg::WARPS - 1) / pg::WARPS;
@@ -602,12 +580,7 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
             if (l < 0) return l;
             c->last_launches = (kp.order ? 4 : 2) + l;
         } else {
-            switch (c->cfg.tie) {
-            case 0: pg::k_ga<0><<<grid, blk, dyn, st>>>(kp); break;
-            case 1: pg::k_ga<1><<<grid, blk, dyn, st>>>(kp); break;
-            case 2: pg::k_ga<2><<<grid, blk, dyn, st>>>(kp); break;
-            default: pg::k_ga<3><<<grid, blk, dyn, st>>>(kp); break;
-            }
+            pg::stat_run(true, c->cfg.tie, kp, grid, dyn, st);
             c->last_launches = kp.order ? 5 : 3;
         }
     } else {
@@ -622,12 +595,7 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
             if (l < 0) return l;
             c->last_launches = (kp.order ? 2 : 0) + l;
         } else {
-            switch (c->cfg.tie) {
-            case 0: pg::k_sw<0><<<grid, blk, dyn, st>>>(kp); break;
-            case 1: pg::k_sw<1><<<grid, blk, dyn, st>>>(kp); break;
-            case 2: pg::k_sw<2><<<grid, blk, dyn, st>>>(kp); break;
-            default: pg::k_sw<3><<<grid, blk, dyn, st>>>(kp); break;
-            }
+            pg::stat_run(false, c->cfg.tie, kp, grid, dyn, st);
             c->last_launches = kp.order ? 3 : 1;
         }
     }
@@ -767,7 +735,7 @@ int pg_set_tuning(pg_ctx *c, const pg_tuning *t)
     if (t->rows_max < 1 || t->rows_max > 8) return fail(PG_ERR_ARG, "rows_max %d outside 1..8", t->rows_max);
     if (t->graph != 0 && t->graph != 1) return fail(PG_ERR_ARG, "graph must be 0 or 1");
     if (t->xd_int16 != 0 && t->xd_int16 != 1) return fail(PG_ERR_ARG, "xd_int16 must be 0 or 1");
-    if (t->dp_traceback != 0 && t->dp_traceback != 1) return fail(PG_ERR_ARG, "dp_traceback must be 0 or 1");
+    if (t->dp_traceback < 0 || t->dp_traceback > 2) return fail(PG_ERR_ARG, "dp_traceback must be 0, 1 or 2");
     if (t->dir_arena_mb < 0) return fail(PG_ERR_ARG, "dir_arena_mb must be >= 0");
     c->tune = *t;
     ++c->epoch;                         // launch shapes changed: recapture

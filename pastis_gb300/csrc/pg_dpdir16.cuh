@@ -1,0 +1,312 @@
+// pg_dpdir16.cuh -- the traceback-form DP on 16-bit lanes (sm_103a).
+//
+// dp_warp_dir (pg_dpdir.cuh) with each lane split into two virtual lanes held
+// in the two halves of 32-bit registers: the low half works R rows, the high
+// half the R rows below them one column behind.  A warp is a wavefront of 64
+// virtual lanes (virtual lane v = 2 * lane + half works column k - v + 1 at
+// step k), and each packed max / add (PTX max.s16x2, add.s16x2) computes two
+// cells.  The high half's upper neighbour is the low half of the same lane one
+// step earlier; the low half's is the high half of the lane above, handed down
+// by one __shfl_up_sync of the packed edge.
+//
+// Scores are exact while every value of the region stays inside int16: a
+// region runs here only when (m + n + 4) * maxabs <= 30000, maxabs the largest
+// magnitude among the substitution scores and the two gap scores
+// (dir16_limit), which bounds every H, E, F and their sums (a path of m + n
+// steps).  Larger regions run on the 32-bit lanes of dp_warp_dir.
+//
+// Decisions come from equalities on the packed values, not from predicates:
+// min.u16x2(x ^ y, 1) is 1 in the halves where x != y.  Nibble of cell (i, j):
+//   bit 0   H is not the diagonal (diagonal wins every tie)
+//   bit 1   with bit 0: H is E (else F), under the tie policy's order of F and E
+//   bit 2   E(i, j) was opened from H(i, j-1)
+//   bit 3   F(i, j) was opened from H(i-1, j)
+// A local alignment's floor needs no bit: the traceback carries the score of
+// the cell it stands on and stops where H is 0, which is where the 32-bit
+// form sets its zero code.  Layout: the nibbles of virtual lane v's R rows at
+// column j in word (stripe * (n + 63) + k) * 64 + v, k = j - 1 + v; a lane
+// stores its two virtual lanes' words as one 8-byte store, so a warp writes
+// 256 contiguous bytes per step.
+//
+// Borders need no special case in the loop.  The high half starts one column
+// early, at column 0, from a column -1 of sentinels (H = NEG16) and the
+// sentinel residue (score -128 against every row): the recurrence then gives
+// column 0 itself (global: the vertical gap run down column 0; local: 0).
+// The low half runs one column past n at the end; that column, like the rows
+// past m, is computed from sentinel scores and reaches no cell of the region.
+#pragma once
+#include <cstdint>
+
+#include "pg_dpdir.cuh"
+
+namespace pg {
+
+constexpr int NEG16 = -32000;
+constexpr int SENT16 = NCODES;                 // residue code of column -1 and past n
+constexpr int NC16 = NCODES + 1;
+constexpr int PROF16_BYTES = 2 * NC16 * 32 * 8; // per warp: low and high halves' profiles
+constexpr uint32_t ONE2 = 0x00010001u;
+
+__device__ __forceinline__ uint32_t v16max(uint32_t a, uint32_t b)
+{
+    uint32_t d;
+    asm("max.s16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+__device__ __forceinline__ uint32_t v16add(uint32_t a, uint32_t b)
+{
+    uint32_t d;
+    asm("add.s16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+// 1 in each half where a != b, else 0
+__device__ __forceinline__ uint32_t v16ne(uint32_t a, uint32_t b)
+{
+    uint32_t d;
+    asm("min.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a ^ b), "r"(ONE2));
+    return d;
+}
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t s)
+{
+    uint32_t d;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(s));
+    return d;
+}
+__host__ __device__ __forceinline__ uint32_t pk16(int lo, int hi)
+{
+    return ((uint32_t)lo & 0xffffu) | ((uint32_t)hi << 16);
+}
+__device__ __forceinline__ int lo16(uint32_t x) { return (int)(int16_t)(x & 0xffffu); }
+__device__ __forceinline__ int hi16(uint32_t x) { return (int)(int16_t)(x >> 16); }
+__device__ __forceinline__ int half16(uint32_t x, int h) { return h ? hi16(x) : lo16(x); }
+
+// largest m + n that runs on 16-bit lanes (0: none)
+__host__ __forceinline__ int dir16_limit(int maxabs)
+{
+    if (maxabs < 1) maxabs = 1;
+    if (maxabs > 100) return 0;
+    return 30000 / maxabs - 4;
+}
+
+__host__ __device__ __forceinline__ int dir16_rows(int m, int cap)
+{
+    const int RMAX = cap < 1 ? 1 : (cap > 8 ? 8 : cap);
+    const int stripes = m > 0 ? (m + 64 * RMAX - 1) / (64 * RMAX) : 1;
+    const int r = (m + 64 * stripes - 1) / (64 * stripes);
+    return r < 1 ? 1 : r;
+}
+
+__host__ __device__ __forceinline__ uint64_t dir16_bytes(int m, int n, int R)
+{
+    if (m <= 0 || n <= 0) return 0;
+    const uint64_t stripes = (uint64_t)((m + 64 * R - 1) / (64 * R));
+    return stripes * (uint64_t)(n + 63) * 256ull;
+}
+
+// prmt selectors: row q of each half's word, sign-extended to 16 bits
+__device__ __forceinline__ constexpr uint32_t sx_sel(int q)
+{
+    return (uint32_t)q | ((uint32_t)(q | 8) << 4) | ((uint32_t)(4 + q) << 8) |
+           ((uint32_t)((4 + q) | 8) << 12);
+}
+
+template <int TIE, int R, bool LOCAL>
+__device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
+                                const uint8_t *__restrict__ Hs, int n,
+                                const int *__restrict__ ssm, uint2 *__restrict__ prof,
+                                int go, int ge, EdgeD *__restrict__ bnd, uint32_t *__restrict__ dir)
+{
+    static_assert(R >= 1 && R <= 8, "a direction word holds 8 rows");
+    const int lane = threadIdx.x & 31;
+    constexpr bool E_FIRST = (TIE & TIE_E_BEFORE_F) != 0;
+    constexpr bool OPEN_FIRST = (TIE & TIE_OPEN_FIRST) != 0;
+    const int gmax = go > ge ? go : ge;
+    const uint32_t go2 = pk16(go, go), ge2 = pk16(ge, ge);
+    uint2 *profLo = prof, *profHi = prof + NC16 * 32;
+    int bs = 0, bi = 0, bj = 0;
+    DirOut res;
+    res.have = 0; res.ei = 0; res.ej = 0; res.score = 0;
+    for (int rb = 0, stripe = 0; rb < m; rb += 64 * R, ++stripe) {
+        const int rows_here = min(64 * R, m - rb);
+        const int v_last = (rows_here - 1) / R;
+        const int t_last = v_last >> 1;
+        const bool last_block = rb + rows_here >= m;
+        const bool lane_on = lane <= t_last;
+        const int hi_on = (2 * lane + 1 <= v_last) ? 1 : 0;
+        const int i_base = rb + 2 * lane * R;           // row above the low half
+        // score profile of this lane's 2R rows (pads and the sentinel: -128)
+        __syncwarp();
+        {
+            int vc[2 * R];
+#pragma unroll
+            for (int r = 0; r < 2 * R; ++r) {
+                const int i = i_base + r + 1;
+                vc[r] = (lane_on && i <= m) ? (int)__ldg(V + i - 1) : -1;
+            }
+            for (int q = 0; q < NC16; ++q) {
+                int c = q + lane;
+                if (c >= NC16) c -= NC16;
+                uint32_t w[4] = {0x80808080u, 0x80808080u, 0x80808080u, 0x80808080u};
+                if (c < NCODES) {
+#pragma unroll
+                    for (int r = 0; r < 2 * R; ++r) {
+                        const int h = r / R, rr = r - h * R;
+                        const uint32_t b = vc[r] >= 0 ? ((uint32_t)ssm[vc[r] * 32 + c] & 0xffu) : 0x80u;
+                        const int wi = 2 * h + (rr >> 2), sh = 8 * (rr & 3);
+                        w[wi] = (w[wi] & ~(0xffu << sh)) | (b << sh);
+                    }
+                }
+                profLo[c * 32 + lane] = make_uint2(w[0], w[1]);
+                profHi[c * 32 + lane] = make_uint2(w[2], w[3]);
+            }
+        }
+        __syncwarp();
+        // column 0 of the low half's rows, column -1 (sentinels) of the high half's
+        uint32_t Hl[R], Al[R], Gl[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int h0 = dir_col0<LOCAL>(min(i_base + r + 1, m), go, ge, gmax).h;
+            Hl[r] = pk16(h0, NEG16);
+            Al[r] = pk16(NEG16 + ge, NEG16);
+            Gl[r] = pk16(h0 + go, NEG16 + go);
+        }
+        const EdgeD e_up = dir_col0<LOCAL>(min(i_base, m), go, ge, gmax);
+        const EdgeD e_lo = dir_col0<LOCAL>(min(i_base + R, m), go, ge, gmax);
+        const EdgeD e_hi = dir_col0<LOCAL>(min(i_base + 2 * R, m), go, ge, gmax);
+        uint32_t in_h = pk16(e_up.h, e_lo.h), in_a = pk16(e_up.a, e_lo.a);
+        uint32_t out_h = pk16(e_lo.h, e_hi.h), out_a = pk16(e_lo.a, e_hi.a);
+        const uint32_t in_sel = lane == 0 ? 0x5410u : 0x5432u;
+        // residues: the low half's column at this step, the high half's (one behind)
+        int hc_lo = SENT16;
+        int hc_next = SENT16;
+        {
+            const int j1 = -2 * lane + 1;                // low half's column at step 0
+            if (j1 >= 1 && j1 <= n) hc_next = (int)__ldg(Hs + j1 - 1);
+        }
+        uint2 *dstep = reinterpret_cast<uint2 *>(dir) + (uint64_t)stripe * (uint64_t)(n + 63) * 32u + lane;
+        uint32_t sbs = 0, sbs_seen = 0;
+        int sbp0 = 0, sbp1 = 0;
+        const int nsteps = n + v_last;
+        for (int k = 0; k < nsteps; ++k) {
+            const uint32_t rh = __shfl_up_sync(FULL, out_h, 1);
+            const uint32_t ra = __shfl_up_sync(FULL, out_a, 1);
+            const uint32_t dgH = in_h;
+            const int j = k - 2 * lane + 1;              // low half's column; high half: j - 1
+            uint32_t th = rh, ta = ra;
+            if (lane == 0) {
+                EdgeD e;
+                if (rb == 0) e = dir_row0<LOCAL>(j, go, ge, gmax);
+                else if (j <= n) e = bnd[j];
+                else { e.h = 0; e.a = NEG16; }
+                th = (uint32_t)e.h; ta = (uint32_t)e.a;
+            }
+            in_h = prmt(th, out_h, in_sel);
+            in_a = prmt(ta, out_a, in_sel);
+            const int hc_hi = hc_lo;
+            hc_lo = hc_next;
+            {
+                const int jn = j + 1;
+                hc_next = (jn >= 1 && jn <= n) ? (int)__ldg(Hs + jn - 1) : SENT16;
+            }
+            if (lane_on && j >= 1 && j <= n + hi_on) {
+                const uint2 pl = profLo[hc_lo * 32 + lane];
+                const uint2 ph = profHi[hc_hi * 32 + lane];
+                uint32_t cA = in_a, cG = v16add(in_h, go2);
+                uint32_t dH = dgH;
+                uint32_t W0 = 0, W1 = 0;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const uint32_t s2 = prmt(r < 4 ? pl.x : pl.y, r < 4 ? ph.x : ph.y, sx_sel(r & 3));
+                    const uint32_t E = v16max(Al[r], Gl[r]);
+                    const uint32_t pe = OPEN_FIRST ? (v16ne(E, Gl[r]) ^ ONE2) : v16ne(E, Al[r]);
+                    const uint32_t dg = v16add(dH, s2);
+                    const uint32_t X = v16max(dg, E);
+                    const uint32_t F = v16max(cA, cG);
+                    const uint32_t pf = OPEN_FIRST ? (v16ne(F, cG) ^ ONE2) : v16ne(F, cA);
+                    const uint32_t Hv = LOCAL ? __vimax_s16x2_relu(X, F) : v16max(X, F);
+                    const uint32_t nd = v16ne(Hv, dg);
+                    const uint32_t ne = E_FIRST ? (v16ne(Hv, E) ^ ONE2) : v16ne(Hv, F);
+                    const uint32_t nib = nd + 2u * ne + 4u * pe + 8u * pf;
+                    if (r < 4) W0 += nib << (4 * (r & 3));
+                    else W1 += nib << (4 * (r & 3));
+                    const uint32_t G = v16add(Hv, go2);
+                    cA = v16add(F, ge2);
+                    cG = G;
+                    dH = Hl[r];
+                    Hl[r] = Hv;
+                    Al[r] = v16add(E, ge2);
+                    Gl[r] = G;
+                    if (LOCAL) sbs = v16max(sbs, Hv);
+                }
+                dstep[(uint64_t)k * 32u] = make_uint2(prmt(W0, W1, 0x5410u), prmt(W0, W1, 0x7632u));
+                out_h = Hl[R - 1];
+                out_a = cA;
+                if (!last_block && lane == t_last) {
+                    const int h = v_last & 1;
+                    const int jb = j - h;
+                    if (jb >= 1 && jb <= n) {
+                        EdgeD e;
+                        e.h = half16(out_h, h);
+                        e.a = half16(out_a, h);
+                        bnd[jb] = e;
+                    }
+                }
+                if (LOCAL && sbs != sbs_seen) {
+                    // a new maximum in this column: its first row
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int s = half16(sbs, h);
+                        if (s != half16(sbs_seen, h)) {
+                            int rr = R - 1;
+#pragma unroll
+                            for (int r = R - 1; r >= 0; --r)
+                                if (half16(Hl[r], h) == s) rr = r;
+                            const int p = ((j - h) << 3) | rr;
+                            if (h) sbp1 = p; else sbp0 = p;
+                        }
+                    }
+                    sbs_seen = sbs;
+                }
+            }
+        }
+        __syncwarp();
+        if (LOCAL) {
+            // the low half's rows come before the high half's: a tie keeps the low
+            // half, and against earlier stripes a tie goes to the smaller column
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int s = half16(sbs, h);
+                const int sp = h ? sbp1 : sbp0;
+                const int sj = sp >> 3;
+                if (s > 0 && (s > bs || (s == bs && sj < bj))) {
+                    bs = s; bj = sj; bi = i_base + h * R + (sp & 7) + 1;
+                }
+            }
+        }
+        if (!LOCAL && last_block) {
+            const int rl = (rows_here - 1) % R;
+            const int h = v_last & 1;
+            int hs = 0;
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                if (r == rl) hs = half16(Hl[r], h);
+            res.score = __shfl_sync(FULL, hs, t_last);
+        }
+    }
+    if (LOCAL) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const int os = __shfl_xor_sync(FULL, bs, o);
+            const int oi = __shfl_xor_sync(FULL, bi, o);
+            const int oj = __shfl_xor_sync(FULL, bj, o);
+            const bool take = os > bs || (os == bs && (oj < bj || (oj == bj && oi < bi)));
+            if (take) { bs = os; bi = oi; bj = oj; }
+        }
+        res.score = bs;
+        res.have = bs > 0;
+        res.ei = bi; res.ej = bj;
+    }
+    return res;
+}
+
+}  // namespace pg

@@ -17,6 +17,11 @@
 // --sfa (SW): k_hist, k_bucket, then k_sw, one warp per pair, local
 // alignment with statistics.
 //
+// This file holds the shared parameters and helpers, the schedule and the
+// statistics kernels k_ga / k_sw; the extension kernels are in
+// pg_kernels_xd.cuh, the traceback form of the alignment in
+// pg_kernels_dir.cuh (its own translation unit, pg_dir.cu).
+//
 // All kernels are persistent with work stealing (grids sized to the resident
 // capacity) so pairs of very different lengths balance themselves.
 #pragma once
@@ -24,6 +29,7 @@
 
 #include "../../include/pastis_gb300.h"
 #include "pg_dp.cuh"
+#include "pg_dpdir16.cuh"
 #include "pg_xdrop.cuh"
 
 namespace pg {
@@ -73,6 +79,7 @@ struct KParams {
     const uint32_t *order = nullptr; // pair taken as the t-th task by k_ga / k_sw (null: t)
     int rows_cap = 8;                // cap on DP rows per lane (tuning)
     int dir = 0;                     // 1: the traceback form (pg_kernels_dir.cuh) runs the DP
+    int dir16_lim = 0;               // traceback form: regions with m + n <= this on 16-bit lanes
 };
 
 __device__ __forceinline__ void load_sm(int *ssm, const int8_t *sm)
@@ -162,177 +169,6 @@ __device__ __forceinline__ bool seed_region(const KParams &kp, const pg_pair &pr
     return false;
 }
 
-// ------------------------------------------------------------------ k_xd
-__global__ void __launch_bounds__(XT) k_xd(const KParams kp)
-{
-    __shared__ int ssm[32 * 32];
-    __shared__ int ring[3 * XW * XT];
-    load_sm(ssm, kp.sm);
-    __syncthreads();
-    int *base = ring + threadIdx.x;
-    const uint64_t ntask = 2 * kp.n;
-    unsigned long long exec = 0;
-    for (;;) {
-        const uint64_t task = atomicAdd(&kp.counter[1], 1u);
-        if (task >= ntask) break;
-        const uint64_t p = task >> 1;
-        const int s = (int)(task & 1);
-        const pg_pair pr = kp.pairs[p];
-        XdRec rec{0, 0, 0, 0, 0u, 0u};
-        const uint8_t *V, *Hs;
-        int m, n;
-        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
-            rec.flags = XF_BADIDX;
-        } else if (s >= kp.seed_count ||
-                   (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
-            rec.flags = XF_NONE;
-        } else if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
-            rec.flags = XF_SAME;
-        } else {
-            int bv, ev, bh, eh;
-            if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
-            bool ok = true;
-            if (bv > 0 && bh > 0) {
-                const XdOut x = xdrop_dir_thread<XW, XT>(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1,
-                                                         ssm, kp.xg, kp.xdrop, base);
-                ok = x.ok;
-                rec.cells += x.cells;
-                bv -= x.dv; bh -= x.dh;
-            }
-            if (ok && ev < m && eh < n) {
-                const XdOut x = xdrop_dir_thread<XW, XT>(V + ev, m - ev, 1, Hs + eh, n - eh, 1,
-                                                         ssm, kp.xg, kp.xdrop, base);
-                ok = x.ok;
-                rec.cells += x.cells;
-                ev += x.dv; eh += x.dh;
-            }
-            if (ok) {
-                rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev;
-                rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
-                exec += rec.cells;
-            } else {
-                rec.flags |= XF_OVF;
-                rec.cells = 0;
-                const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
-                kp.ovf[slot] = (uint32_t)task;
-            }
-        }
-        kp.xd[task] = rec;
-    }
-    if (exec) atomicAdd(kp.exec_cells, exec);
-}
-
-// ------------------------------------------------------------- k_xd_wide
-__device__ __forceinline__ XdOut xdrop_dir_any(const uint8_t *V, int nv, int vstep,
-                                               const uint8_t *Hs, int nh, int hstep,
-                                               const int *ssm, int g, int X, int *sring,
-                                               int *gring, int gring_w)
-{
-    XdOut o = xdrop_dir_warp(V, nv, vstep, Hs, nh, hstep, ssm, g, X, sring, RING_W);
-    if (!o.ok) o = xdrop_dir_warp(V, nv, vstep, Hs, nh, hstep, ssm, g, X, gring, gring_w);
-    return o;
-}
-
-// ------------------------------------------------------------------ k_xd16
-// k_xd in 16-bit lanes (xdrop_dir_thread16): two band cells per instruction.
-// A task whose band outgrows the ring or whose score passes SAT16 goes to the
-// overflow list and k_xd_wide reruns it in 32 bits.
-__global__ void __launch_bounds__(XT) k_xd16(const KParams kp)
-{
-    __shared__ int ssm[32 * 32];
-    __shared__ uint32_t ring[3 * 8 * XT];
-    load_sm(ssm, kp.sm);
-    __syncthreads();
-    uint32_t *base = ring + threadIdx.x;
-    const uint64_t ntask = 2 * kp.n;
-    unsigned long long exec = 0;
-    for (;;) {
-        const uint64_t task = atomicAdd(&kp.counter[1], 1u);
-        if (task >= ntask) break;
-        const uint64_t p = task >> 1;
-        const int s = (int)(task & 1);
-        const pg_pair pr = kp.pairs[p];
-        XdRec rec{0, 0, 0, 0, 0u, 0u};
-        const uint8_t *V, *Hs;
-        int m, n;
-        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
-            rec.flags = XF_BADIDX;
-        } else if (s >= kp.seed_count ||
-                   (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
-            rec.flags = XF_NONE;
-        } else if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
-            rec.flags = XF_SAME;
-        } else {
-            int bv, ev, bh, eh;
-            if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
-            bool ok = true;
-            if (bv > 0 && bh > 0) {
-                const XdOut x = xdrop_dir_thread16<XT>(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1,
-                                                       ssm, kp.xg, kp.xdrop, base);
-                ok = x.ok; rec.cells += x.cells; bv -= x.dv; bh -= x.dh;
-            }
-            if (ok && ev < m && eh < n) {
-                const XdOut x = xdrop_dir_thread16<XT>(V + ev, m - ev, 1, Hs + eh, n - eh, 1,
-                                                       ssm, kp.xg, kp.xdrop, base);
-                ok = x.ok; rec.cells += x.cells; ev += x.dv; eh += x.dh;
-            }
-            if (ok) {
-                rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev; rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
-                exec += rec.cells;
-            } else {
-                rec.flags |= XF_OVF;
-                rec.cells = 0;
-                const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
-                kp.ovf[slot] = (uint32_t)task;
-            }
-        }
-        kp.xd[task] = rec;
-    }
-    if (exec) atomicAdd(kp.exec_cells, exec);   // index 0 = X-drop cells
-}
-
-__global__ void __launch_bounds__(WARPS * 32) k_xd_wide(const KParams kp)
-{
-    __shared__ int ssm[32 * 32];
-    __shared__ int sring[WARPS][3 * RING_W];
-    load_sm(ssm, kp.sm);
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const uint64_t gw = (uint64_t)blockIdx.x * WARPS + wib;
-    const uint64_t nw = (uint64_t)gridDim.x * WARPS;
-    int *gring = kp.gring + gw * 3ull * (uint64_t)kp.gring_w;
-    const unsigned int novf = kp.counter[2];
-    unsigned long long exec = 0;
-    for (uint64_t q = gw; q < novf; q += nw) {
-        const uint32_t task = kp.ovf[q];
-        const uint64_t p = task >> 1;
-        const int s = (int)(task & 1);
-        const pg_pair pr = kp.pairs[p];
-        const uint8_t *V, *Hs;
-        int m, n;
-        pair_seqs(kp, pr, V, m, Hs, n);
-        XdRec rec{0, 0, 0, 0, 0u, 0u};
-        int bv, ev, bh, eh;
-        if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
-        if (bv > 0 && bh > 0) {
-            const XdOut x = xdrop_dir_any(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1, ssm, kp.xg,
-                                          kp.xdrop, sring[wib], gring, kp.gring_w);
-            rec.cells += x.cells;
-            bv -= x.dv; bh -= x.dh;
-        }
-        if (ev < m && eh < n) {
-            const XdOut x = xdrop_dir_any(V + ev, m - ev, 1, Hs + eh, n - eh, 1, ssm, kp.xg,
-                                          kp.xdrop, sring[wib], gring, kp.gring_w);
-            rec.cells += x.cells;
-            ev += x.dv; eh += x.dh;
-        }
-        rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev; rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
-        exec += rec.cells;
-        if (lane == 0) kp.xd[task] = rec;
-    }
-    if (lane == 0 && exec) atomicAdd(kp.exec_cells, exec);
-}
-
 // ------------------------------------------------------------------ k_ga
 // Rows per lane by region height.  A stripe of 32*R rows costs (n + last
 // busy lane) column steps of R cells whatever number of its lanes hold rows,
@@ -378,9 +214,22 @@ __device__ __forceinline__ DpOut<S> dp_dispatch(const uint8_t *V, int m, const u
 // instantiations together are larger than the instruction cache, and mixing
 // them measured 1.4x slower.  Costly pairs also start first, so cheap ones
 // fill the tail of the batch.
-constexpr int NBUCKET = 16;
+constexpr int NBUCKET = 24;
 constexpr int SCHED_WORDS = 2 * NBUCKET;
-constexpr int BUCKET_NONE = 12;   // no DP work
+constexpr int BUCKET_NONE = 23;   // no DP work
+
+// traceback form: 16-bit lanes for this region (pg_dpdir16.cuh)?
+__host__ __device__ __forceinline__ bool dir16_use(const KParams &kp, int m, int n)
+{
+    return m > 0 && n > 0 && m + n <= kp.dir16_lim;
+}
+
+// traceback form: rows per lane of the region's DP, 16-bit lanes (12..19) after 32-bit (4..11)
+__device__ __forceinline__ int dir_bucket(const KParams &kp, int m, int n)
+{
+    if (dir16_use(kp, m, n)) return 20 - dir16_rows(m, kp.rows_cap);
+    return 12 - dp_rows_per_lane<S1>(m, kp.rows_cap);
+}
 
 // bucket of the first seed's region (X-drop) or of the pair (SW)
 template <bool XDROP>
@@ -394,14 +243,14 @@ __device__ __forceinline__ int pair_bucket(const KParams &kp, uint64_t p)
         n = r.eh - r.bh;
         if (m <= 0 || n <= 0) return BUCKET_NONE;
         // the traceback form has no statistics words: one family up to 8 rows
-        if (kp.dir) return 12 - dp_rows_per_lane<S1>(m, kp.rows_cap);                             // 4..11
+        if (kp.dir) return dir_bucket(kp, m, n);                                                     // 4..19
         if (m > S1::MAXSIDE || n > S1::MAXSIDE) return 4 - dp_rows_per_lane<S2>(m, kp.rows_cap);   // 0..3
         return 12 - dp_rows_per_lane<S1>(m, kp.rows_cap);                                           // 4..11
     }
     const pg_pair pr = kp.pairs[p];
     const uint8_t *V, *Hs;
     if (!pair_seqs(kp, pr, V, m, Hs, n) || m == 0 || n == 0) return BUCKET_NONE;
-    if (kp.dir) return 12 - dp_rows_per_lane<S1>(m, kp.rows_cap);                                  // 4..11
+    if (kp.dir) return dir_bucket(kp, m, n);                                                          // 4..19
     if (m > L1::MAXSIDE || n > L1::MAXSIDE) return 4 - dp_rows_per_lane<L2>(m, kp.rows_cap);        // 0..3
     return 8 - dp_rows_per_lane<L1>(m, kp.rows_cap);                                                // 4..7
 }
@@ -455,6 +304,7 @@ __global__ void __launch_bounds__(256) k_bucket(const KParams kp)
 
 // dynamic shared memory of the warp-per-pair kernels: one score profile per warp
 constexpr int DP_DYN_SMEM = WARPS * PROF_BYTES;
+constexpr int DIR16_DYN_SMEM = WARPS * PROF16_BYTES;   // the traceback form with 16-bit lanes
 extern __shared__ uint2 g_dyn_prof[];
 
 template <int TIE>

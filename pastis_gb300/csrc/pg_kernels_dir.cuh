@@ -1,6 +1,7 @@
 // pg_kernels_dir.cuh -- the traceback form of the alignment kernels (tuning
-// option dp_traceback): k_ga_dir / k_sw_dir run dp_warp_dir (one warp per
-// pair, direction nibbles into an HBM arena), k_tb_ga / k_tb_sw trace them
+// option dp_traceback): k_ga_dir / k_sw_dir run dp_warp_dir, or dp_warp_dir16
+// on 16-bit lanes for the regions that fit them (dp_traceback 2; one warp per
+// region, direction nibbles into an HBM arena), k_tb_ga / k_tb_sw trace them
 // back (one thread per pair) and write the same pg_result records k_ga /
 // k_sw write.  A batch whose direction matrices exceed the arena runs in
 // chunks of consecutive tasks (bucket order), each chunk DP then traceback.
@@ -8,6 +9,7 @@
 #include <cstdint>
 
 #include "pg_dpdir.cuh"
+#include "pg_dpdir16.cuh"
 #include "pg_kernels.cuh"
 #include "pg_trace.cuh"
 
@@ -37,10 +39,23 @@ __device__ __forceinline__ SeedPlan seed_plan(const KParams &kp, uint64_t p)
     return sp;
 }
 
-__device__ __forceinline__ uint64_t region_dir_bytes(const XdRec &r, int cap)
+// direction bytes of an m x n region: 16-bit lanes where it fits, else 32-bit
+__device__ __forceinline__ uint64_t region_bytes(const KParams &kp, int m, int n)
 {
-    const int m = r.ev - r.bv, n = r.eh - r.bh;
-    return dir_bytes(m, n, dir_rows(m, cap));
+    if (dir16_use(kp, m, n)) return dir16_bytes(m, n, dir16_rows(m, kp.rows_cap));
+    return dir_bytes(m, n, dir_rows(m, kp.rows_cap));
+}
+
+__device__ __forceinline__ uint64_t region_dir_bytes(const KParams &kp, const XdRec &r)
+{
+    return region_bytes(kp, r.ev - r.bv, r.eh - r.bh);
+}
+
+// this warp's score profile in the dynamic shared memory of the traceback DP
+__device__ __forceinline__ uint2 *dir_prof(const KParams &kp)
+{
+    const int per_warp = (kp.dir16_lim > 0 ? PROF16_BYTES : PROF_BYTES) / 8;
+    return g_dyn_prof + (threadIdx.x >> 5) * per_warp;
 }
 
 // direction bytes of each task (bucket position t)
@@ -55,13 +70,13 @@ __global__ void k_dirsize(const KParams kp, uint64_t *bytes)
         if (p < kp.n) {
             if (XDROP) {
                 const SeedPlan sp = seed_plan(kp, p);
-                if (sp.dp[0]) b += region_dir_bytes(sp.rec[0], kp.rows_cap);
-                if (sp.dp[1]) b += region_dir_bytes(sp.rec[1], kp.rows_cap);
+                if (sp.dp[0]) b += region_dir_bytes(kp, sp.rec[0]);
+                if (sp.dp[1]) b += region_dir_bytes(kp, sp.rec[1]);
             } else {
                 const pg_pair pr = kp.pairs[p];
                 const uint8_t *V, *Hs;
                 int m, n;
-                if (pair_seqs(kp, pr, V, m, Hs, n)) b = dir_bytes(m, n, dir_rows(m, kp.rows_cap));
+                if (pair_seqs(kp, pr, V, m, Hs, n)) b = region_bytes(kp, m, n);
             }
         }
         bytes[t] = b;
@@ -85,11 +100,24 @@ __global__ void k_chunk_end(const uint64_t *doff, uint64_t t0, uint64_t n, uint6
 }
 
 template <int TIE, bool LOCAL>
-__device__ __forceinline__ DirOut dp_dispatch_dir(const uint8_t *V, int m, const uint8_t *Hs, int n,
-                                                  const int *ssm, uint2 *prof, int go, int ge,
-                                                  void *bnd, uint32_t *dir, int cap)
+__device__ __forceinline__ DirOut dp_dispatch_dir(const KParams &kp, const uint8_t *V, int m,
+                                                  const uint8_t *Hs, int n, const int *ssm,
+                                                  uint2 *prof, void *bnd, uint32_t *dir)
 {
     EdgeD *b = (EdgeD *)bnd;
+    const int go = kp.go, ge = kp.ge, cap = kp.rows_cap;
+    if (dir16_use(kp, m, n)) {
+        switch (dir16_rows(m, cap)) {
+        case 1: return dp_warp_dir16<TIE, 1, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+        case 2: return dp_warp_dir16<TIE, 2, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+        case 3: return dp_warp_dir16<TIE, 3, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+        case 4: return dp_warp_dir16<TIE, 4, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+        case 5: return dp_warp_dir16<TIE, 5, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+        case 6: return dp_warp_dir16<TIE, 6, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+        case 7: return dp_warp_dir16<TIE, 7, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+        default: return dp_warp_dir16<TIE, 8, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+        }
+    }
     switch (dir_rows(m, cap)) {
     case 1: return dp_warp_dir<TIE, 1, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
     case 2: return dp_warp_dir<TIE, 2, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
@@ -114,7 +142,7 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga_dir(const KParams kp, uint
     __syncthreads();
     const uint64_t gw = (uint64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
     void *bnd = (char *)kp.bnd + gw * kp.bnd_bytes;
-    uint2 *prof = g_dyn_prof + (threadIdx.x >> 5) * (NCODES * 32);
+    uint2 *prof = dir_prof(kp);
     const int lane = threadIdx.x & 31;
     unsigned long long exec = 0;
     const uint64_t base = doff[t0];
@@ -135,12 +163,11 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga_dir(const KParams kp, uint
             if (!sp.dp[s]) continue;
             const XdRec &r = sp.rec[s];
             const int rm = r.ev - r.bv, rn = r.eh - r.bh;
-            const DirOut d = dp_dispatch_dir<TIE, false>(V + r.bv, rm, Hs + r.bh, rn, ssm, prof, kp.go,
-                                                         kp.ge, bnd, (uint32_t *)(arena + off),
-                                                         kp.rows_cap);
+            const DirOut d = dp_dispatch_dir<TIE, false>(kp, V + r.bv, rm, Hs + r.bh, rn, ssm, prof,
+                                                         bnd, (uint32_t *)(arena + off));
             if (lane == 0) dsc[2 * p + s] = d.score;
             exec += (uint64_t)rm * (uint64_t)rn;
-            off += dir_bytes(rm, rn, dir_rows(rm, kp.rows_cap));
+            off += region_bytes(kp, rm, rn);
         }
     }
     if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
@@ -191,11 +218,14 @@ __global__ void __launch_bounds__(256) k_tb_ga(const KParams kp, uint64_t t0, ui
             uint32_t M = 0, D = 0, G = 0;
             if (rm > 0 && rn > 0) {
                 score = dsc[2 * p + s];
-                const int R = dir_rows(rm, kp.rows_cap);
-                const TraceOut tr = trace_back<false>((const uint32_t *)(arena + off), rn, R, rm, rn,
-                                                      V + bv, Hs + bh);
+                const uint32_t *dm = (const uint32_t *)(arena + off);
+                const TraceOut tr =
+                    dir16_use(kp, rm, rn)
+                        ? trace_back16<false>(dm, rn, dir16_rows(rm, kp.rows_cap), rm, rn, V + bv, Hs + bh,
+                                              kp.sm, kp.go, kp.ge, score)
+                        : trace_back<false>(dm, rn, dir_rows(rm, kp.rows_cap), rm, rn, V + bv, Hs + bh);
                 M = tr.M; D = tr.D; G = tr.G;
-                off += dir_bytes(rm, rn, R);
+                off += region_bytes(kp, rm, rn);
             } else if (rm + rn > 0) {
                 score = kp.go + (rm + rn - 1) * gmax;   // one gap run
                 G = 1;
@@ -235,7 +265,7 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint
     __syncthreads();
     const uint64_t gw = (uint64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
     void *bnd = (char *)kp.bnd + gw * kp.bnd_bytes;
-    uint2 *prof = g_dyn_prof + (threadIdx.x >> 5) * (NCODES * 32);
+    uint2 *prof = dir_prof(kp);
     const int lane = threadIdx.x & 31;
     unsigned long long exec = 0;
     const uint64_t base = doff[t0];
@@ -253,8 +283,8 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint
         DirOut d;
         d.score = 0; d.ei = 0; d.ej = 0; d.have = 0;
         if (m > 0 && n > 0)
-            d = dp_dispatch_dir<TIE, true>(V, m, Hs, n, ssm, prof, kp.go, kp.ge, bnd,
-                                           (uint32_t *)(arena + (doff[t] - base)), kp.rows_cap);
+            d = dp_dispatch_dir<TIE, true>(kp, V, m, Hs, n, ssm, prof, bnd,
+                                           (uint32_t *)(arena + (doff[t] - base)));
         if (lane == 0) {
             int4 *o = reinterpret_cast<int4 *>(dsc) + p;
             *o = make_int4(d.score, d.ei, d.ej, d.have);
@@ -286,9 +316,12 @@ __global__ void __launch_bounds__(256) k_tb_sw(const KParams kp, uint64_t t0, ui
         o.cells = sat_u32((uint64_t)m * (uint64_t)n);
         const int4 d = reinterpret_cast<const int4 *>(dsc)[p];
         if (m > 0 && n > 0 && d.w) {
-            const int R = dir_rows(m, kp.rows_cap);
-            const TraceOut tr = trace_back<true>((const uint32_t *)(arena + (doff[t] - base)), n, R,
-                                                 d.y, d.z, V, Hs);
+            const uint32_t *dm = (const uint32_t *)(arena + (doff[t] - base));
+            const TraceOut tr =
+                dir16_use(kp, m, n)
+                    ? trace_back16<true>(dm, n, dir16_rows(m, kp.rows_cap), d.y, d.z, V, Hs, kp.sm, kp.go,
+                                         kp.ge, d.x)
+                    : trace_back<true>(dm, n, dir_rows(m, kp.rows_cap), d.y, d.z, V, Hs);
             const uint32_t L = (uint32_t)((d.y - tr.i0) + (d.z - tr.j0)) - tr.D;
             o.score = d.x;
             o.aln_len = L; o.matches = tr.M; o.gap_opens = tr.G;

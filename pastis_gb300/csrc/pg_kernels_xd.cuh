@@ -1,0 +1,183 @@
+// pg_kernels_xd.cuh -- the X-drop extension kernels (one definition: only
+// pg_api.cu includes this file): k_xd, thread per (pair, seed) task with the
+// 32-bit band (pg_xdrop.cuh); k_xd16, the same on 16-bit lanes; k_xd_wide,
+// warp per task for the bands that overflow a thread's ring.
+#pragma once
+#include <cstdint>
+
+#include "pg_kernels.cuh"
+
+namespace pg {
+
+// ------------------------------------------------------------------ k_xd
+__global__ void __launch_bounds__(XT) k_xd(const KParams kp)
+{
+    __shared__ int ssm[32 * 32];
+    __shared__ int ring[3 * XW * XT];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
+    int *base = ring + threadIdx.x;
+    const uint64_t ntask = 2 * kp.n;
+    unsigned long long exec = 0;
+    for (;;) {
+        const uint64_t task = atomicAdd(&kp.counter[1], 1u);
+        if (task >= ntask) break;
+        const uint64_t p = task >> 1;
+        const int s = (int)(task & 1);
+        const pg_pair pr = kp.pairs[p];
+        XdRec rec{0, 0, 0, 0, 0u, 0u};
+        const uint8_t *V, *Hs;
+        int m, n;
+        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
+            rec.flags = XF_BADIDX;
+        } else if (s >= kp.seed_count ||
+                   (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
+            rec.flags = XF_NONE;
+        } else if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
+            rec.flags = XF_SAME;
+        } else {
+            int bv, ev, bh, eh;
+            if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
+            bool ok = true;
+            if (bv > 0 && bh > 0) {
+                const XdOut x = xdrop_dir_thread<XW, XT>(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1,
+                                                         ssm, kp.xg, kp.xdrop, base);
+                ok = x.ok;
+                rec.cells += x.cells;
+                bv -= x.dv; bh -= x.dh;
+            }
+            if (ok && ev < m && eh < n) {
+                const XdOut x = xdrop_dir_thread<XW, XT>(V + ev, m - ev, 1, Hs + eh, n - eh, 1,
+                                                         ssm, kp.xg, kp.xdrop, base);
+                ok = x.ok;
+                rec.cells += x.cells;
+                ev += x.dv; eh += x.dh;
+            }
+            if (ok) {
+                rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev;
+                rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
+                exec += rec.cells;
+            } else {
+                rec.flags |= XF_OVF;
+                rec.cells = 0;
+                const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
+                kp.ovf[slot] = (uint32_t)task;
+            }
+        }
+        kp.xd[task] = rec;
+    }
+    if (exec) atomicAdd(kp.exec_cells, exec);
+}
+
+// ------------------------------------------------------------- k_xd_wide
+__device__ __forceinline__ XdOut xdrop_dir_any(const uint8_t *V, int nv, int vstep,
+                                               const uint8_t *Hs, int nh, int hstep,
+                                               const int *ssm, int g, int X, int *sring,
+                                               int *gring, int gring_w)
+{
+    XdOut o = xdrop_dir_warp(V, nv, vstep, Hs, nh, hstep, ssm, g, X, sring, RING_W);
+    if (!o.ok) o = xdrop_dir_warp(V, nv, vstep, Hs, nh, hstep, ssm, g, X, gring, gring_w);
+    return o;
+}
+
+// ------------------------------------------------------------------ k_xd16
+// k_xd in 16-bit lanes (xdrop_dir_thread16): two band cells per instruction.
+// A task whose band outgrows the ring or whose score passes SAT16 goes to the
+// overflow list and k_xd_wide reruns it in 32 bits.
+__global__ void __launch_bounds__(XT) k_xd16(const KParams kp)
+{
+    __shared__ int ssm[32 * 32];
+    __shared__ uint32_t ring[3 * 8 * XT];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
+    uint32_t *base = ring + threadIdx.x;
+    const uint64_t ntask = 2 * kp.n;
+    unsigned long long exec = 0;
+    for (;;) {
+        const uint64_t task = atomicAdd(&kp.counter[1], 1u);
+        if (task >= ntask) break;
+        const uint64_t p = task >> 1;
+        const int s = (int)(task & 1);
+        const pg_pair pr = kp.pairs[p];
+        XdRec rec{0, 0, 0, 0, 0u, 0u};
+        const uint8_t *V, *Hs;
+        int m, n;
+        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
+            rec.flags = XF_BADIDX;
+        } else if (s >= kp.seed_count ||
+                   (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
+            rec.flags = XF_NONE;
+        } else if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
+            rec.flags = XF_SAME;
+        } else {
+            int bv, ev, bh, eh;
+            if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
+            bool ok = true;
+            if (bv > 0 && bh > 0) {
+                const XdOut x = xdrop_dir_thread16<XT>(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1,
+                                                       ssm, kp.xg, kp.xdrop, base);
+                ok = x.ok; rec.cells += x.cells; bv -= x.dv; bh -= x.dh;
+            }
+            if (ok && ev < m && eh < n) {
+                const XdOut x = xdrop_dir_thread16<XT>(V + ev, m - ev, 1, Hs + eh, n - eh, 1,
+                                                       ssm, kp.xg, kp.xdrop, base);
+                ok = x.ok; rec.cells += x.cells; ev += x.dv; eh += x.dh;
+            }
+            if (ok) {
+                rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev; rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
+                exec += rec.cells;
+            } else {
+                rec.flags |= XF_OVF;
+                rec.cells = 0;
+                const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
+                kp.ovf[slot] = (uint32_t)task;
+            }
+        }
+        kp.xd[task] = rec;
+    }
+    if (exec) atomicAdd(kp.exec_cells, exec);   // index 0 = X-drop cells
+}
+
+__global__ void __launch_bounds__(WARPS * 32) k_xd_wide(const KParams kp)
+{
+    __shared__ int ssm[32 * 32];
+    __shared__ int sring[WARPS][3 * RING_W];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint64_t gw = (uint64_t)blockIdx.x * WARPS + wib;
+    const uint64_t nw = (uint64_t)gridDim.x * WARPS;
+    int *gring = kp.gring + gw * 3ull * (uint64_t)kp.gring_w;
+    const unsigned int novf = kp.counter[2];
+    unsigned long long exec = 0;
+    for (uint64_t q = gw; q < novf; q += nw) {
+        const uint32_t task = kp.ovf[q];
+        const uint64_t p = task >> 1;
+        const int s = (int)(task & 1);
+        const pg_pair pr = kp.pairs[p];
+        const uint8_t *V, *Hs;
+        int m, n;
+        pair_seqs(kp, pr, V, m, Hs, n);
+        XdRec rec{0, 0, 0, 0, 0u, 0u};
+        int bv, ev, bh, eh;
+        if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
+        if (bv > 0 && bh > 0) {
+            const XdOut x = xdrop_dir_any(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1, ssm, kp.xg,
+                                          kp.xdrop, sring[wib], gring, kp.gring_w);
+            rec.cells += x.cells;
+            bv -= x.dv; bh -= x.dh;
+        }
+        if (ev < m && eh < n) {
+            const XdOut x = xdrop_dir_any(V + ev, m - ev, 1, Hs + eh, n - eh, 1, ssm, kp.xg,
+                                          kp.xdrop, sring[wib], gring, kp.gring_w);
+            rec.cells += x.cells;
+            ev += x.dv; eh += x.dh;
+        }
+        rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev; rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
+        exec += rec.cells;
+        if (lane == 0) kp.xd[task] = rec;
+    }
+    if (lane == 0 && exec) atomicAdd(kp.exec_cells, exec);
+}
+
+}  // namespace pg

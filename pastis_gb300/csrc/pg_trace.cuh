@@ -14,6 +14,7 @@
 #pragma once
 #include <cstdint>
 
+#include "../../include/pastis_gb300.h"
 #include "pg_dpdir.cuh"
 
 namespace pg {
@@ -66,6 +67,70 @@ __device__ TraceOut trace_back(const uint32_t *__restrict__ dir, int n, int R, i
             if (last != 2) ++G;
             last = 2;
             state = (nib & DIR_EOPEN) ? 0 : 2;
+            --j;
+        }
+    }
+    TraceOut o;
+    o.M = M; o.D = D; o.G = G; o.i0 = i; o.j0 = j;
+    return o;
+}
+
+// Traceback over the nibbles of dp_warp_dir16 (pg_dpdir16.cuh): the same walk
+// and counts as trace_back.  Bit 0 of a nibble says H is not the diagonal,
+// bit 1 then picks E over F; a local walk carries the value of the state it
+// stands on (h: the end cell's score, less each diagonal's substitution score,
+// plus the gap score a gap move undoes) and stops at an H-state cell whose
+// value is 0, the cells the 32-bit form marks with its zero code.  sm is the
+// PG_NRES x PG_NRES substitution table.
+template <bool LOCAL>
+__device__ TraceOut trace_back16(const uint32_t *__restrict__ dir, int n, int R, int i, int j,
+                                 const uint8_t *__restrict__ V, const uint8_t *__restrict__ Hs,
+                                 const int8_t *__restrict__ sm, int go, int ge, int h)
+{
+    uint32_t M = 0, D = 0, G = 0;
+    int state = 0;   // 0: H, 1: F (vertical gap), 2: E (horizontal gap)
+    int last = 0;    // orientation of the previous move: 0 diagonal / none, 1 vertical, 2 horizontal
+    const int rows = 64 * R;
+    for (;;) {
+        if (i == 0 || j == 0) {
+            if (!LOCAL) {
+                if (i > 0 && last != 1) ++G;
+                else if (j > 0 && last != 2) ++G;
+            }
+            break;
+        }
+        if (LOCAL && state == 0 && h == 0) break;
+        const int r0 = i - 1;
+        const int stripe = r0 / rows, within = r0 - stripe * rows;
+        const int v = within / R, r = within - v * R;
+        const uint32_t w = __ldg(dir + ((uint64_t)stripe * (uint64_t)(n + 63) +
+                                        (uint64_t)(j - 1 + v)) * 64u + v);
+        const uint32_t nib = (w >> (4 * r)) & 15u;
+        if (state == 0) {
+            if (!(nib & 1u)) {
+                const int a = __ldg(V + i - 1), b = __ldg(Hs + j - 1);
+                ++D;
+                M += a == b ? 1u : 0u;
+                if (LOCAL) h -= (a < PG_NRES && b < PG_NRES) ? (int)__ldg(sm + a * PG_NRES + b) : 0;
+                --i; --j;
+                last = 0;
+                continue;
+            }
+            state = (nib & 2u) ? 2 : 1;
+        }
+        if (state == 1) {
+            if (last != 1) ++G;
+            last = 1;
+            const bool open = (nib & DIR_FOPEN) != 0;
+            if (LOCAL) h -= open ? go : ge;
+            state = open ? 0 : 1;
+            --i;
+        } else {
+            if (last != 2) ++G;
+            last = 2;
+            const bool open = (nib & DIR_EOPEN) != 0;
+            if (LOCAL) h -= open ? go : ge;
+            state = open ? 0 : 2;
             --j;
         }
     }

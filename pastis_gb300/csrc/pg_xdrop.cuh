@@ -32,7 +32,7 @@ struct XdOut {
 };
 
 // V / Hs point at the first residue to consume; vstep / hstep are +1 or -1.
-__device__ XdOut xdrop_dir_warp(const uint8_t *__restrict__ V, int nv, int vstep,
+__device__ inline XdOut xdrop_dir_warp(const uint8_t *__restrict__ V, int nv, int vstep,
                                 const uint8_t *__restrict__ Hs, int nh, int hstep,
                                 const int *__restrict__ ssm, int g, int X,
                                 int *ring, int W)

@@ -257,7 +257,9 @@ def test_tuning_and_graph_replay_keep_results(native, oracle_mod, mode):
               {"xd_blocks_per_sm": 2}, {"graph": 1}, {"graph": 1, "bucket_order": 0},
               {"xd_int16": 1}, {"xd_int16": 1, "graph": 1}, {"dp_traceback": 1},
               {"dp_traceback": 1, "dir_arena_mb": 1}, {"dp_traceback": 1, "rows_max": 3},
-              {"dp_traceback": 1, "bucket_order": 0, "graph": 1}):
+              {"dp_traceback": 1, "bucket_order": 0, "graph": 1}, {"dp_traceback": 2},
+              {"dp_traceback": 2, "dir_arena_mb": 1}, {"dp_traceback": 2, "rows_max": 3},
+              {"dp_traceback": 2, "bucket_order": 0}):
         ctx.set_tuning(capi.default_tuning(), **t)
         for rep in range(2):                 # the second call replays the graph
             got = ctx.align(w.pairs)
@@ -320,16 +322,18 @@ def test_int16_extension_saturation_reruns_in_32_bits(native, oracle_mod):
 @pytest.mark.parametrize("tie", [0, 1, 2, 3])
 @pytest.mark.parametrize("gaps", [0, 1])
 @pytest.mark.parametrize("mode", [0, 1])
-def test_traceback_form_parity(sw_small, xd_small, oracle_mod, tie, gaps, mode):
+@pytest.mark.parametrize("form", [1, 2])
+def test_traceback_form_parity(sw_small, xd_small, oracle_mod, tie, gaps, mode, form):
     """The traceback form of the DP (direction nibbles in HBM, then a walk
-    back) gives the oracle's results under every tie policy and gap model."""
+    back), on 32-bit lanes (form 1) and 16-bit lanes (form 2), gives the
+    oracle's results under every tie policy and gap model."""
     from pastis_gb300 import capi
     w = sw_small if mode == capi.MODE_SW else xd_small
     cfg = capi.config(mode, tie=tie, gap_semantics=gaps)
     ctx = capi.Context(cfg)
     ctx.set_seqs(0, w.ascii, w.offs)
     ctx.share_row_seqs()
-    ctx.set_tuning(dp_traceback=1)
+    ctx.set_tuning(dp_traceback=form)
     got = ctx.align(w.pairs)
     O = oracle_mod
     codes = O.encode(bytes(w.ascii))
@@ -340,19 +344,54 @@ def test_traceback_form_parity(sw_small, xd_small, oracle_mod, tie, gaps, mode):
 
 def test_traceback_form_long_regions(native, oracle_mod):
     """Regions over 1023 rows and columns (several stripes of 256 rows, the
-    wide-statistics case of the other form), both modes, small arena chunks."""
+    wide-statistics case of the other form), both modes, small arena chunks;
+    in form 2 the regions over the 16-bit limit (m + n > 2723 with BLOSUM62)
+    share the batch with 16-bit ones of several stripes of 64 R rows."""
     from pastis_gb300 import capi, synth
     w = synth.generate("uneven10m", seed=5, scale=0.00003)
     O = oracle_mod
     codes = O.encode(bytes(w.ascii))
     for mode in (capi.MODE_SW, capi.MODE_XDROP):
         cfg = capi.config(mode)
-        ctx = capi.Context(cfg)
-        ctx.set_seqs(0, w.ascii, w.offs)
-        ctx.share_row_seqs()
-        ctx.set_tuning(dp_traceback=1, dir_arena_mb=2)
-        got = ctx.align(w.pairs)
         exp = O.batch(mode, codes, w.offs, codes, w.offs, w.pairs, oracle_params(O, cfg))
-        assert_same(got, exp, w.pairs)
-        ctx.close()
+        for form in (1, 2):
+            ctx = capi.Context(cfg)
+            ctx.set_seqs(0, w.ascii, w.offs)
+            ctx.share_row_seqs()
+            ctx.set_tuning(dp_traceback=form, dir_arena_mb=2)
+            got = ctx.align(w.pairs)
+            assert_same(got, exp, w.pairs)
+            ctx.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("scale", [8, 10])
+def test_traceback16_limit_splits_the_batch(sw_small, xd_small, oracle_mod, mode, scale):
+    """A substitution table scaled by 8 (largest magnitude 88) leaves 16-bit
+    lanes only to regions with m + n <= 336, so one batch runs on both lane
+    widths; scaled by 10 (magnitude 110) no region qualifies.  Results equal
+    the oracle's run with the same table."""
+    from pastis_gb300 import capi
+    O = oracle_mod
+    w = sw_small if mode == capi.MODE_SW else xd_small
+    sm = np.ascontiguousarray(O.blosum62().astype(np.int32) * scale).clip(-127, 127).astype(np.int8)
+    cfg = capi.config(mode)
+    cfg.score_matrix = sm.ctypes.data
+    ctx = capi.Context(cfg)
+    ctx.set_seqs(0, w.ascii, w.offs)
+    ctx.share_row_seqs()
+    ctx.set_tuning(dp_traceback=2)
+    got = ctx.align(w.pairs)
+    codes = O.encode(bytes(w.ascii))
+    first, ext, xg = capi.resolved_gaps(cfg)
+    p = O.make_params(gap_first=first, gap_ext=ext, xdrop_gap=xg, xdrop=cfg.xdrop,
+                      seed_len=cfg.seed_len, seed_count=cfg.seed_count, tie=cfg.tie,
+                      flags=cfg.flags, cov_thr=cfg.cov_thr, ani_thr=cfg.ani_thr, sm=sm)
+    exp = O.batch(mode, codes, w.offs, codes, w.offs, w.pairs, p)
+    assert_same(got, exp, w.pairs)
+    lens = np.diff(w.offs.astype(np.int64))
+    tot = lens[w.pairs["row"]] + lens[w.pairs["col"]]
+    if scale == 8 and mode == capi.MODE_SW:
+        assert (tot <= 336).any() and (tot > 336).any()
+    ctx.close()
 
