@@ -144,7 +144,8 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
                 vc[r] = (lane_on && i <= m) ? (int)__ldg(V + i - 1) : -1;
             }
             for (int q = 0; q < NC16; ++q) {
-                int c = q + lane;
+                int c = q + lane;            // q + lane < 2 * NC16 + 6: up to two wraps
+                if (c >= NC16) c -= NC16;
                 if (c >= NC16) c -= NC16;
                 uint32_t w[4] = {0x80808080u, 0x80808080u, 0x80808080u, 0x80808080u};
                 if (c < NCODES) {
