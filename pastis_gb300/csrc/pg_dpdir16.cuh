@@ -76,6 +76,8 @@ __host__ __device__ __forceinline__ uint32_t pk16(int lo, int hi)
 {
     return ((uint32_t)lo & 0xffffu) | ((uint32_t)hi << 16);
 }
+// a border value of the 32-bit helpers (whose sentinel is NEG = -2^30) in 16 bits
+__device__ __forceinline__ int c16(int x) { return x < NEG16 ? NEG16 : x; }
 __device__ __forceinline__ int lo16(uint32_t x) { return (int)(int16_t)(x & 0xffffu); }
 __device__ __forceinline__ int hi16(uint32_t x) { return (int)(int16_t)(x >> 16); }
 __device__ __forceinline__ int half16(uint32_t x, int h) { return h ? hi16(x) : lo16(x); }
@@ -174,8 +176,8 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
         const EdgeD e_up = dir_col0<LOCAL>(min(i_base, m), go, ge, gmax);
         const EdgeD e_lo = dir_col0<LOCAL>(min(i_base + R, m), go, ge, gmax);
         const EdgeD e_hi = dir_col0<LOCAL>(min(i_base + 2 * R, m), go, ge, gmax);
-        uint32_t in_h = pk16(e_up.h, e_lo.h), in_a = pk16(e_up.a, e_lo.a);
-        uint32_t out_h = pk16(e_lo.h, e_hi.h), out_a = pk16(e_lo.a, e_hi.a);
+        uint32_t in_h = pk16(e_up.h, e_lo.h), in_a = pk16(c16(e_up.a), c16(e_lo.a));
+        uint32_t out_h = pk16(e_lo.h, e_hi.h), out_a = pk16(c16(e_lo.a), c16(e_hi.a));
         const uint32_t in_sel = lane == 0 ? 0x5410u : 0x5432u;
         // residues: the low half's column at this step, the high half's (one behind)
         int hc_lo = SENT16;
@@ -199,7 +201,7 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
                 if (rb == 0) e = dir_row0<LOCAL>(j, go, ge, gmax);
                 else if (j <= n) e = bnd[j];
                 else { e.h = 0; e.a = NEG16; }
-                th = (uint32_t)e.h; ta = (uint32_t)e.a;
+                th = (uint32_t)c16(e.h); ta = (uint32_t)c16(e.a);
             }
             in_h = prmt(th, out_h, in_sel);
             in_a = prmt(ta, out_a, in_sel);

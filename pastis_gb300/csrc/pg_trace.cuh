@@ -24,6 +24,36 @@ struct TraceOut {
     int i0, j0;
 };
 
+// The direction words of a region as a walk reads them: word (s * (n + VL -
+// 1) + k) * VL + v of stripe s, step k, lane v (VL = 32 lanes, or 64 virtual
+// lanes).  A walk only moves to smaller k and smaller v, so a miss loads a
+// tile of TK steps x 4 lanes ending at the missed word (TK independent 16-byte
+// loads, one memory round trip) and the next steps read it from the tile
+// until the walk leaves it: about TK steps per round trip instead of one.
+template <int VL>
+struct DirTile {
+    static constexpr int TK = 8;
+    const uint32_t *dir;
+    int n;
+    uint4 t[TK];
+    int ts = -1, tk0 = 0, tvb = -1;
+    __device__ __forceinline__ DirTile(const uint32_t *d, int n_) : dir(d), n(n_) {}
+    __device__ __forceinline__ uint32_t get(int s, int k, int v)
+    {
+        const int vb = v & ~3;
+        if (s != ts || vb != tvb || k > tk0 || k <= tk0 - TK) {
+            ts = s; tvb = vb; tk0 = k;
+            const uint4 *b = reinterpret_cast<const uint4 *>(dir + (uint64_t)s * (uint64_t)(n + VL - 1) * VL + vb);
+#pragma unroll
+            for (int q = 0; q < TK; ++q)
+                t[q] = k - q >= 0 ? __ldg(b + (uint64_t)(k - q) * (VL / 4)) : make_uint4(0u, 0u, 0u, 0u);
+        }
+        const uint4 w = t[tk0 - k];
+        const int c = v - vb;
+        return c == 0 ? w.x : (c == 1 ? w.y : (c == 2 ? w.z : w.w));
+    }
+};
+
 template <bool LOCAL>
 __device__ TraceOut trace_back(const uint32_t *__restrict__ dir, int n, int R, int i, int j,
                                const uint8_t *__restrict__ V, const uint8_t *__restrict__ Hs)
@@ -32,6 +62,7 @@ __device__ TraceOut trace_back(const uint32_t *__restrict__ dir, int n, int R, i
     int state = 0;   // 0: H, 1: F (vertical gap), 2: E (horizontal gap)
     int last = 0;    // orientation of the previous move: 0 diagonal / none, 1 vertical, 2 horizontal
     const int rows = 32 * R;
+    DirTile<32> tile(dir, n);
     for (;;) {
         if (i == 0 || j == 0) {
             if (!LOCAL) {
@@ -43,8 +74,7 @@ __device__ TraceOut trace_back(const uint32_t *__restrict__ dir, int n, int R, i
         const int r0 = i - 1;
         const int stripe = r0 / rows, within = r0 - stripe * rows;
         const int lane = within / R, r = within - lane * R;
-        const uint32_t w = __ldg(dir + ((uint64_t)stripe * (uint64_t)(n + 31) +
-                                        (uint64_t)(j - 1 + lane)) * 32u + lane);
+        const uint32_t w = tile.get(stripe, j - 1 + lane, lane);
         const uint32_t nib = (w >> (4 * r)) & 15u;
         if (state == 0) {
             const uint32_t hs = nib & 3u;
@@ -91,6 +121,7 @@ __device__ TraceOut trace_back16(const uint32_t *__restrict__ dir, int n, int R,
     int state = 0;   // 0: H, 1: F (vertical gap), 2: E (horizontal gap)
     int last = 0;    // orientation of the previous move: 0 diagonal / none, 1 vertical, 2 horizontal
     const int rows = 64 * R;
+    DirTile<64> tile(dir, n);
     for (;;) {
         if (i == 0 || j == 0) {
             if (!LOCAL) {
@@ -103,8 +134,7 @@ __device__ TraceOut trace_back16(const uint32_t *__restrict__ dir, int n, int R,
         const int r0 = i - 1;
         const int stripe = r0 / rows, within = r0 - stripe * rows;
         const int v = within / R, r = within - v * R;
-        const uint32_t w = __ldg(dir + ((uint64_t)stripe * (uint64_t)(n + 63) +
-                                        (uint64_t)(j - 1 + v)) * 64u + v);
+        const uint32_t w = tile.get(stripe, j - 1 + v, v);
         const uint32_t nib = (w >> (4 * r)) & 15u;
         if (state == 0) {
             if (!(nib & 1u)) {
