@@ -311,12 +311,18 @@ def run_gpu(args, rank, world, local_rank):
     line = None
     if rank == 0:
         peak_ops = capi.dpx_peak(dev)
-        peak_gcups = peak_ops / DPX_OPS_PER_CELL / 1e9
+        form = ctx.get_tuning().dp_traceback
+        # 16-bit lanes: each packed op advances two cells, so the same op rate
+        # bounds twice the cells (the conservative peak for a mixed batch)
+        cells_per_op = 2 if form == 2 else 1
+        peak_gcups = peak_ops * cells_per_op / DPX_OPS_PER_CELL / 1e9
         # dominant kernel: the alignment DP (k_ga / k_sw), its own cells and time
         achieved = exec_dp / (dp_ms * 1e-3) / 1e9
         traffic = None
-        dp_kernel = (("k_ga_dir + k_tb_ga" if mode else "k_sw_dir + k_tb_sw")
-                     if ctx.get_tuning().dp_traceback else ("k_ga" if mode else "k_sw"))
+        dp_kernel = {0: "k_ga" if mode else "k_sw",
+                     1: "k_ga_dir + k_tb_ga" if mode else "k_sw_dir + k_tb_sw",
+                     2: ("k_ga_dir + k_tb_ga" if mode else "k_sw_dir + k_tb_sw")
+                     + " (16-bit lanes)"}[form]
         tpath = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tpath):
             # ncu DRAM bytes per pair of the same kernel on this workload
@@ -361,7 +367,10 @@ def run_gpu(args, rank, world, local_rank):
                          "kernel": dp_kernel,
                          "kernel_ms": dp_ms, "kernel_cells": exec_dp,
                          "peak_source": "measured %.4g DPX add-max/s (pg_dpx_peak) / %d "
-                                        "int32 DPX ops per cell" % (peak_ops, DPX_OPS_PER_CELL),
+                                        "DPX ops per cell%s" % (
+                                            peak_ops, DPX_OPS_PER_CELL,
+                                            ", x 2 cells per packed 16-bit op" if form == 2
+                                            else " (int32)"),
                          "hbm": {"achieved_GBps": hbm_gbs,
                                  "peak_GBps": peaks.get("hbm_gbs"),
                                  "frac": hbm_gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs")

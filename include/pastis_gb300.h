@@ -189,8 +189,10 @@ typedef struct pg_tuning {
     int32_t dir_arena_mb;       /* cap on that arena in MiB; 0 = a third of the device memory */
 } pg_tuning;                    /* 32 bytes */
 
-/* The built-in tuning; a new context starts from it, with dp_traceback on for
- * PG_MODE_SW (measured faster there, slower for the X-drop global alignment). */
+/* The built-in tuning.  A new context starts from it with dp_traceback = 2
+ * (measured fastest in both modes); with a score table whose magnitudes pass
+ * 100 (no region fits 16 bits) it takes 1 for PG_MODE_SW and keeps 0 for
+ * PG_MODE_XDROP. */
 void pg_tuning_default(pg_tuning *t);
 int  pg_get_tuning(const pg_ctx *ctx, pg_tuning *out);
 /* PG_ERR_ARG on a value out of range. */

@@ -321,9 +321,12 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     c->dp_per_sm = std::max(per_sm, 1);
     c->xd_per_sm = c->grid_xd ? c->grid_xd / c->nsm : 1;
     pg_tuning_default(&c->tune);
-    // local alignment in the traceback form measured 1.47x faster (sw100k:
-    // 24.7 -> 16.8 ms); the X-drop global alignment is faster with statistics
-    if (cfg->mode == PG_MODE_SW) c->tune.dp_traceback = 1;
+    // The traceback form on 16-bit lanes measured fastest in both modes (DP
+    // phase, sw100k: statistics 24.7 ms, 32-bit traceback 18.1 ms, 16-bit
+    // 10.9 ms; xdrop1m: 72.8 / 78.6 / 57.9 ms).  With a score table too wide
+    // for 16 bits every region would take 32-bit lanes, where the X-drop
+    // global alignment is faster with statistics.
+    c->tune.dp_traceback = c->lim16 > 0 ? 2 : (cfg->mode == PG_MODE_SW ? 1 : 0);
 #undef CUD
     *out = c;
     return PG_OK;
