@@ -2,7 +2,7 @@
 // option dp_traceback): k_ga_dir / k_sw_dir run dp_warp_dir, or dp_warp_dir16
 // on 16-bit lanes for the regions that fit them (dp_traceback 2; one warp per
 // region, direction nibbles into an HBM arena), k_tb_ga / k_tb_sw trace them
-// back (one thread per pair) and write the same pg_result records k_ga /
+// back (one warp per pair, pg_trace.cuh) and write the same pg_result records k_ga /
 // k_sw write.  A batch whose direction matrices exceed the arena runs in
 // chunks of consecutive tasks (bucket order), each chunk DP then traceback.
 #pragma once
@@ -173,32 +173,35 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga_dir(const KParams kp, uint
     if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
 }
 
-// traceback and result of the tasks [t0, t1), one thread per task: the same
-// record k_ga writes
-__global__ void __launch_bounds__(256) k_tb_ga(const KParams kp, uint64_t t0, uint64_t t1,
+// traceback and result of the tasks [t0, t1), one warp per task (every lane
+// the same walk, lane 0 writes): the same record k_ga writes
+__global__ void __launch_bounds__(256, 3) k_tb_ga(const KParams kp, uint64_t t0, uint64_t t1,
                                                const uint64_t *doff, const uint8_t *arena,
                                                const int *dsc)
 {
+    __shared__ int ssm[32 * 32];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
     const uint64_t base = doff[t0];
     const int gmax = kp.go > kp.ge ? kp.go : kp.ge;
-    for (uint64_t t = t0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < t1;
-         t += (uint64_t)gridDim.x * blockDim.x) {
+    const bool lead = (threadIdx.x & 31) == 0;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t t = t0 + (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < t1; t += warps) {
         const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
-        if (p >= kp.n) { atomicOr(kp.status, ST_BAD_SCHED); continue; }
+        if (p >= kp.n) { if (lead) atomicOr(kp.status, ST_BAD_SCHED); continue; }
         const pg_pair pr = kp.pairs[p];
         const uint8_t *V, *Hs;
         int m, n;
         pg_result best = empty_result();
         if (!pair_seqs(kp, pr, V, m, Hs, n)) {
-            atomicOr(kp.status, ST_BAD_INDEX);
-            kp.out[p] = best;
+            if (lead) { atomicOr(kp.status, ST_BAD_INDEX); kp.out[p] = best; }
             continue;
         }
         const SeedPlan sp = seed_plan(kp, p);
         uint64_t off = doff[t] - base;
         uint64_t cells = 0;
         bool have = false, bad = false;
-#pragma unroll
+#pragma unroll 1
         for (int s = 0; s < 2; ++s) {
             const XdRec &rec = sp.rec[s];
             if (rec.flags & XF_NONE) continue;
@@ -221,9 +224,10 @@ __global__ void __launch_bounds__(256) k_tb_ga(const KParams kp, uint64_t t0, ui
                 const uint32_t *dm = (const uint32_t *)(arena + off);
                 const TraceOut tr =
                     dir16_use(kp, rm, rn)
-                        ? trace_back16<false>(dm, rn, dir16_rows(rm, kp.rows_cap), rm, rn, V + bv, Hs + bh,
-                                              kp.sm, kp.go, kp.ge, score)
-                        : trace_back<false>(dm, rn, dir_rows(rm, kp.rows_cap), rm, rn, V + bv, Hs + bh);
+                        ? trace_walk<false, true>(dm, rn, dir16_rows(rm, kp.rows_cap), rm, rn, V + bv, rm,
+                                                  Hs + bh, ssm, kp.go, kp.ge, score)
+                        : trace_walk<false, false>(dm, rn, dir_rows(rm, kp.rows_cap), rm, rn, V + bv, rm,
+                                                   Hs + bh, ssm, kp.go, kp.ge, score);
                 M = tr.M; D = tr.D; G = tr.G;
                 off += region_bytes(kp, rm, rn);
             } else if (rm + rn > 0) {
@@ -250,7 +254,7 @@ __global__ void __launch_bounds__(256) k_tb_ga(const KParams kp, uint64_t t0, ui
         best.cells = sat_u32(cells);
         if (bad) best.flags |= PG_RF_BAD_SEED;
         apply_filter(best, m, n, kp.cov_thr, kp.ani_thr);
-        kp.out[p] = best;
+        if (lead) kp.out[p] = best;
     }
 }
 
@@ -293,24 +297,27 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint
     if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
 }
 
-// traceback and result of the tasks [t0, t1), one thread per task: the same
-// record k_sw writes
-__global__ void __launch_bounds__(256) k_tb_sw(const KParams kp, uint64_t t0, uint64_t t1,
+// traceback and result of the tasks [t0, t1), one warp per task (every lane
+// the same walk, lane 0 writes): the same record k_sw writes
+__global__ void __launch_bounds__(256, 4) k_tb_sw(const KParams kp, uint64_t t0, uint64_t t1,
                                                const uint64_t *doff, const uint8_t *arena,
                                                const int *dsc)
 {
+    __shared__ int ssm[32 * 32];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
     const uint64_t base = doff[t0];
-    for (uint64_t t = t0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < t1;
-         t += (uint64_t)gridDim.x * blockDim.x) {
+    const bool lead = (threadIdx.x & 31) == 0;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t t = t0 + (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < t1; t += warps) {
         const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
-        if (p >= kp.n) { atomicOr(kp.status, ST_BAD_SCHED); continue; }
+        if (p >= kp.n) { if (lead) atomicOr(kp.status, ST_BAD_SCHED); continue; }
         const pg_pair pr = kp.pairs[p];
         const uint8_t *V, *Hs;
         int m, n;
         pg_result o = empty_result();
         if (!pair_seqs(kp, pr, V, m, Hs, n)) {
-            atomicOr(kp.status, ST_BAD_INDEX);
-            kp.out[p] = o;
+            if (lead) { atomicOr(kp.status, ST_BAD_INDEX); kp.out[p] = o; }
             continue;
         }
         o.cells = sat_u32((uint64_t)m * (uint64_t)n);
@@ -319,9 +326,10 @@ __global__ void __launch_bounds__(256) k_tb_sw(const KParams kp, uint64_t t0, ui
             const uint32_t *dm = (const uint32_t *)(arena + (doff[t] - base));
             const TraceOut tr =
                 dir16_use(kp, m, n)
-                    ? trace_back16<true>(dm, n, dir16_rows(m, kp.rows_cap), d.y, d.z, V, Hs, kp.sm, kp.go,
-                                         kp.ge, d.x)
-                    : trace_back<true>(dm, n, dir_rows(m, kp.rows_cap), d.y, d.z, V, Hs);
+                    ? trace_walk<true, true>(dm, n, dir16_rows(m, kp.rows_cap), d.y, d.z, V, m, Hs, ssm,
+                                             kp.go, kp.ge, d.x)
+                    : trace_walk<true, false>(dm, n, dir_rows(m, kp.rows_cap), d.y, d.z, V, m, Hs, ssm,
+                                              kp.go, kp.ge, d.x);
             const uint32_t L = (uint32_t)((d.y - tr.i0) + (d.z - tr.j0)) - tr.D;
             o.score = d.x;
             o.aln_len = L; o.matches = tr.M; o.gap_opens = tr.G;
@@ -330,7 +338,7 @@ __global__ void __launch_bounds__(256) k_tb_sw(const KParams kp, uint64_t t0, ui
             if (L > 0) { o.identity = identity_of(tr.M, L); o.flags = 0; }
         }
         apply_filter(o, m, n, kp.cov_thr, kp.ani_thr);
-        kp.out[p] = o;
+        if (lead) kp.out[p] = o;
     }
 }
 

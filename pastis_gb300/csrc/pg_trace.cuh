@@ -1,8 +1,9 @@
 // pg_trace.cuh -- traceback over the direction nibbles of dp_warp_dir
-// (pg_dpdir.cuh): one thread walks one region from its end cell back to its
-// start and counts what computeAlignmentStats counts
-// (src/align/SeqanFullAligner.cpp:238-246): diagonal columns, identical
-// columns, and gap runs (maximal runs of same-orientation gap moves).
+// (pg_dpdir.cuh, 32 lanes) or dp_warp_dir16 (pg_dpdir16.cuh, 64 virtual
+// lanes): a walk from the region's end cell back to its start that counts
+// what computeAlignmentStats counts (src/align/SeqanFullAligner.cpp:238-246):
+// diagonal columns, identical columns, and gap runs (maximal runs of
+// same-orientation gap moves).
 //
 // The walk follows the DP's own decisions, so its path is the one whose
 // statistics dp_warp carries to the end cell: H-state cells move as their
@@ -11,6 +12,17 @@
 // when its gap was opened.  Borders: a global alignment reaching row 0 or
 // column 0 finishes along it in one gap run; a local alignment stops there,
 // or at a cell whose H fell to 0, and starts at that cell.
+//
+// One warp walks one region, every lane the same walk (uniform control
+// flow).  A walk is a chain of dependent reads, one per step, so the warp
+// reads ahead in tiles: the direction words of 32 wavefront steps x 8 lanes
+// (one 16-byte load per lane, one memory round trip) and 128 residues of
+// each sequence (4 per lane); each step takes its word or residue from the
+// tile with a shuffle, and only a step that leaves a tile pays a round trip
+// (a walk moves to smaller steps, lanes and residues only).  One thread per
+// region with a word load per step measured slower: every step waited on
+// memory, and a per-thread tile misses somewhere in the warp at nearly every
+// step.
 #pragma once
 #include <cstdint>
 
@@ -24,104 +36,91 @@ struct TraceOut {
     int i0, j0;
 };
 
-// The direction words of a region as a walk reads them: word (s * (n + VL -
-// 1) + k) * VL + v of stripe s, step k, lane v (VL = 32 lanes, or 64 virtual
-// lanes).  A walk only moves to smaller k and smaller v, so a miss loads a
-// tile of TK steps x 4 lanes ending at the missed word (TK independent 16-byte
-// loads, one memory round trip) and the next steps read it from the tile
-// until the walk leaves it: about TK steps per round trip instead of one.
+// Direction words of a region: word (s * (n + VL - 1) + k) * VL + v of stripe
+// s, wavefront step k, lane v (VL = 32 lanes, or 64 virtual lanes).  Lane L
+// holds the 4 words of lanes vb + 4 (L & 1) .. + 3 at steps k0 - (L >> 1) and
+// k0 - 16 - (L >> 1).
 template <int VL>
-struct DirTile {
-    static constexpr int TK = 8;
+struct WarpDirTile {
     const uint32_t *dir;
     int n;
-    uint4 t[TK];
+    uint4 a, b;
     int ts = -1, tk0 = 0, tvb = -1;
-    __device__ __forceinline__ DirTile(const uint32_t *d, int n_) : dir(d), n(n_) {}
+    __device__ __forceinline__ WarpDirTile(const uint32_t *d, int n_) : dir(d), n(n_) {}
     __device__ __forceinline__ uint32_t get(int s, int k, int v)
     {
-        const int vb = v & ~3;
-        if (s != ts || vb != tvb || k > tk0 || k <= tk0 - TK) {
+        const int vb = v & ~7;
+        if (s != ts || vb != tvb || k > tk0 || k < tk0 - 31) {
             ts = s; tvb = vb; tk0 = k;
-            const uint4 *b = reinterpret_cast<const uint4 *>(dir + (uint64_t)s * (uint64_t)(n + VL - 1) * VL + vb);
-#pragma unroll
-            for (int q = 0; q < TK; ++q)
-                t[q] = k - q >= 0 ? __ldg(b + (uint64_t)(k - q) * (VL / 4)) : make_uint4(0u, 0u, 0u, 0u);
+            const int lane = threadIdx.x & 31;
+            const uint32_t *row = dir + (uint64_t)s * (uint64_t)(n + VL - 1) * VL + vb + 4 * (lane & 1);
+            const int k1 = k - (lane >> 1), k2 = k1 - 16;
+            a = k1 >= 0 ? __ldg(reinterpret_cast<const uint4 *>(row + (uint64_t)k1 * VL)) : make_uint4(0u, 0u, 0u, 0u);
+            b = k2 >= 0 ? __ldg(reinterpret_cast<const uint4 *>(row + (uint64_t)k2 * VL)) : make_uint4(0u, 0u, 0u, 0u);
         }
-        const uint4 w = t[tk0 - k];
-        const int c = v - vb;
-        return c == 0 ? w.x : (c == 1 ? w.y : (c == 2 ? w.z : w.w));
+        const int d = v - vb, idx = tk0 - k;
+        const uint4 q = idx < 16 ? a : b;
+        const int c = d & 3;
+        const uint32_t mine = c == 0 ? q.x : (c == 1 ? q.y : (c == 2 ? q.z : q.w));
+        return __shfl_sync(FULL, mine, ((idx & 15) << 1) | (d >> 2));
     }
 };
 
-template <bool LOCAL>
-__device__ TraceOut trace_back(const uint32_t *__restrict__ dir, int n, int R, int i, int j,
-                               const uint8_t *__restrict__ V, const uint8_t *__restrict__ Hs)
-{
-    uint32_t M = 0, D = 0, G = 0;
-    int state = 0;   // 0: H, 1: F (vertical gap), 2: E (horizontal gap)
-    int last = 0;    // orientation of the previous move: 0 diagonal / none, 1 vertical, 2 horizontal
-    const int rows = 32 * R;
-    DirTile<32> tile(dir, n);
-    for (;;) {
-        if (i == 0 || j == 0) {
-            if (!LOCAL) {
-                if (i > 0 && last != 1) ++G;
-                else if (j > 0 && last != 2) ++G;
-            }
-            break;
+// residues [base, base + 128) of a sequence of len residues, 4 per lane
+struct WarpResidues {
+    const uint8_t *seq;
+    int len;
+    uint32_t w = 0;
+    int base = -(1 << 30);
+    __device__ __forceinline__ WarpResidues(const uint8_t *s, int l) : seq(s), len(l) {}
+    __device__ __forceinline__ int get(int p)     // 0 <= p < len
+    {
+        if (p < base || p >= base + 128) {
+            base = p >= 127 ? p - 127 : 0;        // walks move to smaller p
+            const int q0 = base + 4 * (threadIdx.x & 31);
+            uint32_t x = 0;
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (q0 + c < len) x |= (uint32_t)__ldg(seq + q0 + c) << (8 * c);
+            w = x;
         }
-        const int r0 = i - 1;
-        const int stripe = r0 / rows, within = r0 - stripe * rows;
-        const int lane = within / R, r = within - lane * R;
-        const uint32_t w = tile.get(stripe, j - 1 + lane, lane);
-        const uint32_t nib = (w >> (4 * r)) & 15u;
-        if (state == 0) {
-            const uint32_t hs = nib & 3u;
-            if (hs == DIR_ZERO) break;
-            if (hs == DIR_DIAG) {
-                ++D;
-                M += __ldg(V + i - 1) == __ldg(Hs + j - 1) ? 1u : 0u;
-                --i; --j;
-                last = 0;
-                continue;
-            }
-            state = hs == DIR_F ? 1 : 2;
-        }
-        if (state == 1) {
-            if (last != 1) ++G;
-            last = 1;
-            state = (nib & DIR_FOPEN) ? 0 : 1;
-            --i;
-        } else {
-            if (last != 2) ++G;
-            last = 2;
-            state = (nib & DIR_EOPEN) ? 0 : 2;
-            --j;
-        }
+        const int d = p - base;
+        return (int)((__shfl_sync(FULL, w, d >> 2) >> (8 * (d & 3))) & 0xffu);
     }
-    TraceOut o;
-    o.M = M; o.D = D; o.G = G; o.i0 = i; o.j0 = j;
-    return o;
-}
+};
 
-// Traceback over the nibbles of dp_warp_dir16 (pg_dpdir16.cuh): the same walk
-// and counts as trace_back.  Bit 0 of a nibble says H is not the diagonal,
-// bit 1 then picks E over F; a local walk carries the value of the state it
-// stands on (h: the end cell's score, less each diagonal's substitution score,
-// plus the gap score a gap move undoes) and stops at an H-state cell whose
-// value is 0, the cells the 32-bit form marks with its zero code.  sm is the
-// PG_NRES x PG_NRES substitution table.
-template <bool LOCAL>
-__device__ TraceOut trace_back16(const uint32_t *__restrict__ dir, int n, int R, int i, int j,
-                                 const uint8_t *__restrict__ V, const uint8_t *__restrict__ Hs,
-                                 const int8_t *__restrict__ sm, int go, int ge, int h)
+// The walk, called by all 32 lanes with the same arguments; every lane
+// returns the same counts.  W16: the nibbles of dp_warp_dir16 (bit 0: not the
+// diagonal, bit 1: E rather than F; a local walk carries the score of the
+// cell it stands on, h, and stops where it is 0).  Otherwise the nibbles of
+// dp_warp_dir (bits 0-1: diagonal, F, E or the local floor).  ssm: the 32 x
+// 32 substitution table in shared memory (read only by a local W16 walk).
+template <bool LOCAL, bool W16>
+__device__ TraceOut trace_walk(const uint32_t *__restrict__ dir, int n, int R, int i, int j,
+                               const uint8_t *__restrict__ V, int m, const uint8_t *__restrict__ Hs,
+                               const int *__restrict__ ssm, int go, int ge, int h)
 {
+    constexpr int VL = W16 ? 64 : 32;
     uint32_t M = 0, D = 0, G = 0;
     int state = 0;   // 0: H, 1: F (vertical gap), 2: E (horizontal gap)
     int last = 0;    // orientation of the previous move: 0 diagonal / none, 1 vertical, 2 horizontal
-    const int rows = 64 * R;
-    DirTile<64> tile(dir, n);
+    WarpDirTile<VL> tile(dir, n);
+    WarpResidues rv(V, m), rh(Hs, n);
+    // row i - 1 as stripe s, lane v, row r of the lane (kept in step with i)
+    int s = 0, v = 0, r = 0;
+    if (i > 0) {
+        const int r0 = i - 1, rows = VL * R;
+        s = r0 / rows;
+        const int within = r0 - s * rows;
+        v = within / R;
+        r = within - v * R;
+    }
+    auto up = [&]() {
+        if (--r < 0) {
+            r = R - 1;
+            if (--v < 0) { v = VL - 1; --s; }
+        }
+    };
     for (;;) {
         if (i == 0 || j == 0) {
             if (!LOCAL) {
@@ -130,39 +129,43 @@ __device__ TraceOut trace_back16(const uint32_t *__restrict__ dir, int n, int R,
             }
             break;
         }
-        if (LOCAL && state == 0 && h == 0) break;
-        const int r0 = i - 1;
-        const int stripe = r0 / rows, within = r0 - stripe * rows;
-        const int v = within / R, r = within - v * R;
-        const uint32_t w = tile.get(stripe, j - 1 + v, v);
-        const uint32_t nib = (w >> (4 * r)) & 15u;
+        if (W16 && LOCAL && state == 0 && h == 0) break;
+        const uint32_t nib = (tile.get(s, j - 1 + v, v) >> (4 * r)) & 15u;
         if (state == 0) {
-            if (!(nib & 1u)) {
-                const int a = __ldg(V + i - 1), b = __ldg(Hs + j - 1);
+            bool diag;
+            if (W16) {
+                diag = !(nib & 1u);
+                if (!diag) state = (nib & 2u) ? 2 : 1;
+            } else {
+                const uint32_t hs = nib & 3u;
+                if (hs == DIR_ZERO) break;
+                diag = hs == DIR_DIAG;
+                if (!diag) state = hs == DIR_F ? 1 : 2;
+            }
+            if (diag) {
+                const int a = rv.get(i - 1), b = rh.get(j - 1);
                 ++D;
                 M += a == b ? 1u : 0u;
-                if (LOCAL) h -= (a < PG_NRES && b < PG_NRES) ? (int)__ldg(sm + a * PG_NRES + b) : 0;
+                if (W16 && LOCAL) h -= ssm[a * 32 + b];
                 --i; --j;
+                up();
                 last = 0;
                 continue;
             }
-            state = (nib & 2u) ? 2 : 1;
         }
+        const bool open = (nib & (state == 1 ? DIR_FOPEN : DIR_EOPEN)) != 0;
+        if (W16 && LOCAL) h -= open ? go : ge;
         if (state == 1) {
             if (last != 1) ++G;
             last = 1;
-            const bool open = (nib & DIR_FOPEN) != 0;
-            if (LOCAL) h -= open ? go : ge;
-            state = open ? 0 : 1;
             --i;
+            up();
         } else {
             if (last != 2) ++G;
             last = 2;
-            const bool open = (nib & DIR_EOPEN) != 0;
-            if (LOCAL) h -= open ? go : ge;
-            state = open ? 0 : 2;
             --j;
         }
+        if (open) state = 0;
     }
     TraceOut o;
     o.M = M; o.D = D; o.G = G; o.i0 = i; o.j0 = j;
