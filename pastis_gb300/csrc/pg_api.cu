@@ -508,7 +508,7 @@ static int run_dir(pg_ctx *c, const pg::KParams &kp, uint64_t n, int grid, cudaS
         CU(cudaMemsetAsync(c->d_counter + 3, 0, sizeof(unsigned int), st));
         const uint64_t nt = t1 - t0;
         const int g = (int)std::min<uint64_t>((uint64_t)grid, (nt + pg::WARPS - 1) / pg::WARPS);
-        const int gt = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (nt + 7) / 8);   // warp per task
+        const int gt = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (nt + 255) / 256);
         pg::dir_run(xdrop, tie, kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc, g, dyn, gt, st);
         CU(cudaGetLastError());
         launches += 2;

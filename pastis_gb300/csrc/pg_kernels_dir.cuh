@@ -2,7 +2,7 @@
 // option dp_traceback): k_ga_dir / k_sw_dir run dp_warp_dir, or dp_warp_dir16
 // on 16-bit lanes for the regions that fit them (dp_traceback 2; one warp per
 // region, direction nibbles into an HBM arena), k_tb_ga / k_tb_sw trace them
-// back (one warp per pair, pg_trace.cuh) and write the same pg_result records k_ga /
+// back (one thread per pair, pg_trace.cuh) and write the same pg_result records k_ga /
 // k_sw write.  A batch whose direction matrices exceed the arena runs in
 // chunks of consecutive tasks (bucket order), each chunk DP then traceback.
 #pragma once
@@ -173,9 +173,28 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga_dir(const KParams kp, uint
     if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
 }
 
-// traceback and result of the tasks [t0, t1), one warp per task (every lane
-// the same walk, lane 0 writes): the same record k_ga writes
-__global__ void __launch_bounds__(256, 3) k_tb_ga(const KParams kp, uint64_t t0, uint64_t t1,
+// both seeds' walks of one pair, stepped together (two independent chains of
+// direction loads in flight per thread)
+template <bool WA, bool WB>
+__device__ __forceinline__ void walk_both(const KParams &kp, const uint32_t *const dm[2], const int rm[2],
+                                          const int rn[2], const uint8_t *const V[2],
+                                          const uint8_t *const Hs[2], const int *ssm,
+                                          const bool act[2], TraceOut tr[2])
+{
+    Walker<false, WA> a(dm[0], rn[0], WA ? dir16_rows(rm[0], kp.rows_cap) : dir_rows(rm[0], kp.rows_cap),
+                        rm[0], rn[0], V[0], Hs[0], ssm, kp.go, kp.ge, 0);
+    Walker<false, WB> b(dm[1], rn[1], WB ? dir16_rows(rm[1], kp.rows_cap) : dir_rows(rm[1], kp.rows_cap),
+                        rm[1], rn[1], V[1], Hs[1], ssm, kp.go, kp.ge, 0);
+    a.done = !act[0];
+    b.done = !act[1];
+    while (a.step() | b.step()) {}
+    tr[0] = a.out();
+    tr[1] = b.out();
+}
+
+// traceback and result of the tasks [t0, t1), one thread per task: the same
+// record k_ga writes
+__global__ void __launch_bounds__(256) k_tb_ga(const KParams kp, uint64_t t0, uint64_t t1,
                                                const uint64_t *doff, const uint8_t *arena,
                                                const int *dsc)
 {
@@ -184,26 +203,33 @@ __global__ void __launch_bounds__(256, 3) k_tb_ga(const KParams kp, uint64_t t0,
     __syncthreads();
     const uint64_t base = doff[t0];
     const int gmax = kp.go > kp.ge ? kp.go : kp.ge;
-    const bool lead = (threadIdx.x & 31) == 0;
-    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
-    for (uint64_t t = t0 + (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < t1; t += warps) {
+    for (uint64_t t = t0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < t1;
+         t += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
-        if (p >= kp.n) { if (lead) atomicOr(kp.status, ST_BAD_SCHED); continue; }
+        if (p >= kp.n) { atomicOr(kp.status, ST_BAD_SCHED); continue; }
         const pg_pair pr = kp.pairs[p];
-        const uint8_t *V, *Hs;
+        const uint8_t *Vs, *Hss;
         int m, n;
         pg_result best = empty_result();
-        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
-            if (lead) { atomicOr(kp.status, ST_BAD_INDEX); kp.out[p] = best; }
+        if (!pair_seqs(kp, pr, Vs, m, Hss, n)) {
+            atomicOr(kp.status, ST_BAD_INDEX);
+            kp.out[p] = best;
             continue;
         }
         const SeedPlan sp = seed_plan(kp, p);
+        // each seed's region, and which of them have a DP to walk back
         uint64_t off = doff[t] - base;
         uint64_t cells = 0;
-        bool have = false, bad = false;
-#pragma unroll 1
+        bool bad = false, use[2], act[2], w16[2];
+        const uint32_t *dm[2];
+        const uint8_t *V[2], *Hs[2];
+        int rm[2], rn[2];
+#pragma unroll
         for (int s = 0; s < 2; ++s) {
             const XdRec &rec = sp.rec[s];
+            use[s] = act[s] = w16[s] = false;
+            rm[s] = rn[s] = 0;
+            dm[s] = nullptr; V[s] = Vs; Hs[s] = Hss;
             if (rec.flags & XF_NONE) continue;
             if (rec.flags & XF_SAME) {
                 const XdRec &r0 = sp.rec[0];
@@ -211,36 +237,48 @@ __global__ void __launch_bounds__(256, 3) k_tb_ga(const KParams kp, uint64_t t0,
                 continue;
             }
             if (rec.flags & XF_BAD) bad = true;
-            const int bv = rec.bv, ev = rec.ev, bh = rec.bh, eh = rec.eh;
-            const int rm = ev - bv, rn = eh - bh;
-            cells += rec.cells + (uint64_t)rm * (uint64_t)rn;
-            const bool same_region = s == 1 && !(sp.rec[0].flags & XF_NONE) && bv == sp.rec[0].bv &&
-                                     ev == sp.rec[0].ev && bh == sp.rec[0].bh && eh == sp.rec[0].eh;
+            rm[s] = rec.ev - rec.bv;
+            rn[s] = rec.eh - rec.bh;
+            cells += rec.cells + (uint64_t)rm[s] * (uint64_t)rn[s];
+            const bool same_region = s == 1 && !(sp.rec[0].flags & XF_NONE) && rec.bv == sp.rec[0].bv &&
+                                     rec.ev == sp.rec[0].ev && rec.bh == sp.rec[0].bh && rec.eh == sp.rec[0].eh;
             if (same_region) continue;
+            use[s] = true;
+            V[s] = Vs + rec.bv;
+            Hs[s] = Hss + rec.bh;
+            if (rm[s] > 0 && rn[s] > 0) {
+                act[s] = true;
+                w16[s] = dir16_use(kp, rm[s], rn[s]);
+                dm[s] = (const uint32_t *)(arena + off);
+                off += region_bytes(kp, rm[s], rn[s]);
+            }
+        }
+        TraceOut tr[2];
+        if (w16[0] && w16[1]) walk_both<true, true>(kp, dm, rm, rn, V, Hs, ssm, act, tr);
+        else if (w16[0]) walk_both<true, false>(kp, dm, rm, rn, V, Hs, ssm, act, tr);
+        else if (w16[1]) walk_both<false, true>(kp, dm, rm, rn, V, Hs, ssm, act, tr);
+        else walk_both<false, false>(kp, dm, rm, rn, V, Hs, ssm, act, tr);
+        bool have = false;
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            if (!use[s]) continue;
+            const XdRec &rec = sp.rec[s];
             int score;
             uint32_t M = 0, D = 0, G = 0;
-            if (rm > 0 && rn > 0) {
+            if (act[s]) {
                 score = dsc[2 * p + s];
-                const uint32_t *dm = (const uint32_t *)(arena + off);
-                const TraceOut tr =
-                    dir16_use(kp, rm, rn)
-                        ? trace_walk<false, true>(dm, rn, dir16_rows(rm, kp.rows_cap), rm, rn, V + bv, rm,
-                                                  Hs + bh, ssm, kp.go, kp.ge, score)
-                        : trace_walk<false, false>(dm, rn, dir_rows(rm, kp.rows_cap), rm, rn, V + bv, rm,
-                                                   Hs + bh, ssm, kp.go, kp.ge, score);
-                M = tr.M; D = tr.D; G = tr.G;
-                off += region_bytes(kp, rm, rn);
-            } else if (rm + rn > 0) {
-                score = kp.go + (rm + rn - 1) * gmax;   // one gap run
+                M = tr[s].M; D = tr[s].D; G = tr[s].G;
+            } else if (rm[s] + rn[s] > 0) {
+                score = kp.go + (rm[s] + rn[s] - 1) * gmax;   // one gap run
                 G = 1;
             } else {
                 score = 0;
             }
-            const uint32_t L = (uint32_t)(rm + rn) - D;
+            const uint32_t L = (uint32_t)(rm[s] + rn[s]) - D;
             pg_result cur;
             cur.score = score; cur.aln_len = L; cur.matches = M; cur.gap_opens = G;
-            cur.beg_v = (uint16_t)bv; cur.end_v = (uint16_t)ev;
-            cur.beg_h = (uint16_t)bh; cur.end_h = (uint16_t)eh;
+            cur.beg_v = rec.bv; cur.end_v = rec.ev;
+            cur.beg_h = rec.bh; cur.end_h = rec.eh;
             cur.seed_used = (uint8_t)s; cur.pad = 0; cur.cells = 0; cur.score_aln = 0.0f;
             if (L == 0) { cur.identity = 0.0f; cur.flags = PG_RF_EMPTY; }
             else { cur.identity = identity_of(M, L); cur.flags = 0; }
@@ -254,7 +292,7 @@ __global__ void __launch_bounds__(256, 3) k_tb_ga(const KParams kp, uint64_t t0,
         best.cells = sat_u32(cells);
         if (bad) best.flags |= PG_RF_BAD_SEED;
         apply_filter(best, m, n, kp.cov_thr, kp.ani_thr);
-        if (lead) kp.out[p] = best;
+        kp.out[p] = best;
     }
 }
 
@@ -297,9 +335,9 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint
     if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
 }
 
-// traceback and result of the tasks [t0, t1), one warp per task (every lane
-// the same walk, lane 0 writes): the same record k_sw writes
-__global__ void __launch_bounds__(256, 4) k_tb_sw(const KParams kp, uint64_t t0, uint64_t t1,
+// traceback and result of the tasks [t0, t1), one thread per task: the same
+// record k_sw writes
+__global__ void __launch_bounds__(256) k_tb_sw(const KParams kp, uint64_t t0, uint64_t t1,
                                                const uint64_t *doff, const uint8_t *arena,
                                                const int *dsc)
 {
@@ -307,17 +345,17 @@ __global__ void __launch_bounds__(256, 4) k_tb_sw(const KParams kp, uint64_t t0,
     load_sm(ssm, kp.sm);
     __syncthreads();
     const uint64_t base = doff[t0];
-    const bool lead = (threadIdx.x & 31) == 0;
-    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
-    for (uint64_t t = t0 + (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < t1; t += warps) {
+    for (uint64_t t = t0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < t1;
+         t += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
-        if (p >= kp.n) { if (lead) atomicOr(kp.status, ST_BAD_SCHED); continue; }
+        if (p >= kp.n) { atomicOr(kp.status, ST_BAD_SCHED); continue; }
         const pg_pair pr = kp.pairs[p];
         const uint8_t *V, *Hs;
         int m, n;
         pg_result o = empty_result();
         if (!pair_seqs(kp, pr, V, m, Hs, n)) {
-            if (lead) { atomicOr(kp.status, ST_BAD_INDEX); kp.out[p] = o; }
+            atomicOr(kp.status, ST_BAD_INDEX);
+            kp.out[p] = o;
             continue;
         }
         o.cells = sat_u32((uint64_t)m * (uint64_t)n);
@@ -326,9 +364,9 @@ __global__ void __launch_bounds__(256, 4) k_tb_sw(const KParams kp, uint64_t t0,
             const uint32_t *dm = (const uint32_t *)(arena + (doff[t] - base));
             const TraceOut tr =
                 dir16_use(kp, m, n)
-                    ? trace_walk<true, true>(dm, n, dir16_rows(m, kp.rows_cap), d.y, d.z, V, m, Hs, ssm,
+                    ? trace_walk<true, true>(dm, n, dir16_rows(m, kp.rows_cap), d.y, d.z, V, Hs, ssm,
                                              kp.go, kp.ge, d.x)
-                    : trace_walk<true, false>(dm, n, dir_rows(m, kp.rows_cap), d.y, d.z, V, m, Hs, ssm,
+                    : trace_walk<true, false>(dm, n, dir_rows(m, kp.rows_cap), d.y, d.z, V, Hs, ssm,
                                               kp.go, kp.ge, d.x);
             const uint32_t L = (uint32_t)((d.y - tr.i0) + (d.z - tr.j0)) - tr.D;
             o.score = d.x;
@@ -338,7 +376,7 @@ __global__ void __launch_bounds__(256, 4) k_tb_sw(const KParams kp, uint64_t t0,
             if (L > 0) { o.identity = identity_of(tr.M, L); o.flags = 0; }
         }
         apply_filter(o, m, n, kp.cov_thr, kp.ani_thr);
-        if (lead) kp.out[p] = o;
+        kp.out[p] = o;
     }
 }
 

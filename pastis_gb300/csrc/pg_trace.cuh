@@ -13,16 +13,12 @@
 // column 0 finishes along it in one gap run; a local alignment stops there,
 // or at a cell whose H fell to 0, and starts at that cell.
 //
-// One warp walks one region, every lane the same walk (uniform control
-// flow).  A walk is a chain of dependent reads, one per step, so the warp
-// reads ahead in tiles: the direction words of 32 wavefront steps x 8 lanes
-// (one 16-byte load per lane, one memory round trip) and 128 residues of
-// each sequence (4 per lane); each step takes its word or residue from the
-// tile with a shuffle, and only a step that leaves a tile pays a round trip
-// (a walk moves to smaller steps, lanes and residues only).  One thread per
-// region with a word load per step measured slower: every step waited on
-// memory, and a per-thread tile misses somewhere in the warp at nearly every
-// step.
+// One thread walks one region, one 4-byte direction word per step (the
+// words sit in HBM: the DP of a whole chunk writes them first).  Two
+// read-ahead schemes measured slower and were dropped: a per-thread tile of
+// 8 steps x 4 lanes (a refill somewhere in the warp at nearly every step,
+// and 8 sectors read per refill), and one warp per region reading 32-step x
+// 8-lane tiles through shuffles (a 32nd of the walks in flight).
 #pragma once
 #include <cstdint>
 
@@ -36,101 +32,62 @@ struct TraceOut {
     int i0, j0;
 };
 
-// Direction words of a region: word (s * (n + VL - 1) + k) * VL + v of stripe
-// s, wavefront step k, lane v (VL = 32 lanes, or 64 virtual lanes).  Lane L
-// holds the 4 words of lanes vb + 4 (L & 1) .. + 3 at steps k0 - (L >> 1) and
-// k0 - 16 - (L >> 1).
-template <int VL>
-struct WarpDirTile {
-    const uint32_t *dir;
-    int n;
-    uint4 a, b;
-    int ts = -1, tk0 = 0, tvb = -1;
-    __device__ __forceinline__ WarpDirTile(const uint32_t *d, int n_) : dir(d), n(n_) {}
-    __device__ __forceinline__ uint32_t get(int s, int k, int v)
-    {
-        const int vb = v & ~7;
-        if (s != ts || vb != tvb || k > tk0 || k < tk0 - 31) {
-            ts = s; tvb = vb; tk0 = k;
-            const int lane = threadIdx.x & 31;
-            const uint32_t *row = dir + (uint64_t)s * (uint64_t)(n + VL - 1) * VL + vb + 4 * (lane & 1);
-            const int k1 = k - (lane >> 1), k2 = k1 - 16;
-            a = k1 >= 0 ? __ldg(reinterpret_cast<const uint4 *>(row + (uint64_t)k1 * VL)) : make_uint4(0u, 0u, 0u, 0u);
-            b = k2 >= 0 ? __ldg(reinterpret_cast<const uint4 *>(row + (uint64_t)k2 * VL)) : make_uint4(0u, 0u, 0u, 0u);
-        }
-        const int d = v - vb, idx = tk0 - k;
-        const uint4 q = idx < 16 ? a : b;
-        const int c = d & 3;
-        const uint32_t mine = c == 0 ? q.x : (c == 1 ? q.y : (c == 2 ? q.z : q.w));
-        return __shfl_sync(FULL, mine, ((idx & 15) << 1) | (d >> 2));
-    }
-};
-
-// residues [base, base + 128) of a sequence of len residues, 4 per lane
-struct WarpResidues {
-    const uint8_t *seq;
-    int len;
-    uint32_t w = 0;
-    int base = -(1 << 30);
-    __device__ __forceinline__ WarpResidues(const uint8_t *s, int l) : seq(s), len(l) {}
-    __device__ __forceinline__ int get(int p)     // 0 <= p < len
-    {
-        if (p < base || p >= base + 128) {
-            base = p >= 127 ? p - 127 : 0;        // walks move to smaller p
-            const int q0 = base + 4 * (threadIdx.x & 31);
-            uint32_t x = 0;
-#pragma unroll
-            for (int c = 0; c < 4; ++c)
-                if (q0 + c < len) x |= (uint32_t)__ldg(seq + q0 + c) << (8 * c);
-            w = x;
-        }
-        const int d = p - base;
-        return (int)((__shfl_sync(FULL, w, d >> 2) >> (8 * (d & 3))) & 0xffu);
-    }
-};
-
-// The walk, called by all 32 lanes with the same arguments; every lane
-// returns the same counts.  W16: the nibbles of dp_warp_dir16 (bit 0: not the
-// diagonal, bit 1: E rather than F; a local walk carries the score of the
+// A walker over one region.  W16: the nibbles of dp_warp_dir16 (bit 0: not
+// the diagonal, bit 1: E rather than F; a local walk carries the score of the
 // cell it stands on, h, and stops where it is 0).  Otherwise the nibbles of
-// dp_warp_dir (bits 0-1: diagonal, F, E or the local floor).  ssm: the 32 x
-// 32 substitution table in shared memory (read only by a local W16 walk).
+// dp_warp_dir (bits 0-1: diagonal, F, E or the local floor).  Words: (s * (n
+// + VL - 1) + k) * VL + v for stripe s, wavefront step k = j - 1 + v, lane v
+// (VL = 32 lanes, or 64 virtual lanes).  ssm: the 32 x 32 substitution table
+// in shared memory (read only by a local W16 walk).  step() makes one move
+// and returns false once the walk has ended; the counts are then final.
 template <bool LOCAL, bool W16>
-__device__ TraceOut trace_walk(const uint32_t *__restrict__ dir, int n, int R, int i, int j,
-                               const uint8_t *__restrict__ V, int m, const uint8_t *__restrict__ Hs,
-                               const int *__restrict__ ssm, int go, int ge, int h)
-{
-    constexpr int VL = W16 ? 64 : 32;
+struct Walker {
+    static constexpr int VL = W16 ? 64 : 32;
+    const uint32_t *dir;
+    const uint8_t *V, *Hs;
+    const int *ssm;
+    int n, R, go, ge;
+    int i, j, h;
+    int s = 0, v = 0, r = 0;   // row i - 1 as stripe, lane, row of the lane (kept in step with i)
+    int state = 0;             // 0: H, 1: F (vertical gap), 2: E (horizontal gap)
+    int last = 0;              // previous move: 0 diagonal / none, 1 vertical, 2 horizontal
     uint32_t M = 0, D = 0, G = 0;
-    int state = 0;   // 0: H, 1: F (vertical gap), 2: E (horizontal gap)
-    int last = 0;    // orientation of the previous move: 0 diagonal / none, 1 vertical, 2 horizontal
-    WarpDirTile<VL> tile(dir, n);
-    WarpResidues rv(V, m), rh(Hs, n);
-    // row i - 1 as stripe s, lane v, row r of the lane (kept in step with i)
-    int s = 0, v = 0, r = 0;
-    if (i > 0) {
-        const int r0 = i - 1, rows = VL * R;
-        s = r0 / rows;
-        const int within = r0 - s * rows;
-        v = within / R;
-        r = within - v * R;
+    bool done = false;
+
+    __device__ __forceinline__ Walker(const uint32_t *dir_, int n_, int R_, int i_, int j_,
+                                      const uint8_t *V_, const uint8_t *Hs_, const int *ssm_,
+                                      int go_, int ge_, int h_)
+        : dir(dir_), V(V_), Hs(Hs_), ssm(ssm_), n(n_), R(R_), go(go_), ge(ge_), i(i_), j(j_), h(h_)
+    {
+        if (i > 0) {
+            const int r0 = i - 1, rows = VL * R;
+            s = r0 / rows;
+            const int within = r0 - s * rows;
+            v = within / R;
+            r = within - v * R;
+        }
     }
-    auto up = [&]() {
+    __device__ __forceinline__ void up()
+    {
         if (--r < 0) {
             r = R - 1;
             if (--v < 0) { v = VL - 1; --s; }
         }
-    };
-    for (;;) {
+    }
+    __device__ __forceinline__ bool step()
+    {
+        if (done) return false;
         if (i == 0 || j == 0) {
             if (!LOCAL) {
                 if (i > 0 && last != 1) ++G;
                 else if (j > 0 && last != 2) ++G;
             }
-            break;
+            done = true;
+            return false;
         }
-        if (W16 && LOCAL && state == 0 && h == 0) break;
-        const uint32_t nib = (tile.get(s, j - 1 + v, v) >> (4 * r)) & 15u;
+        if (W16 && LOCAL && state == 0 && h == 0) { done = true; return false; }
+        const uint32_t w = __ldg(dir + ((uint64_t)s * (uint64_t)(n + VL - 1) + (uint64_t)(j - 1 + v)) * VL + v);
+        const uint32_t nib = (w >> (4 * r)) & 15u;
         if (state == 0) {
             bool diag;
             if (W16) {
@@ -138,19 +95,19 @@ __device__ TraceOut trace_walk(const uint32_t *__restrict__ dir, int n, int R, i
                 if (!diag) state = (nib & 2u) ? 2 : 1;
             } else {
                 const uint32_t hs = nib & 3u;
-                if (hs == DIR_ZERO) break;
+                if (hs == DIR_ZERO) { done = true; return false; }
                 diag = hs == DIR_DIAG;
                 if (!diag) state = hs == DIR_F ? 1 : 2;
             }
             if (diag) {
-                const int a = rv.get(i - 1), b = rh.get(j - 1);
+                const int a = __ldg(V + i - 1), b = __ldg(Hs + j - 1);
                 ++D;
                 M += a == b ? 1u : 0u;
                 if (W16 && LOCAL) h -= ssm[a * 32 + b];
                 --i; --j;
                 up();
                 last = 0;
-                continue;
+                return true;
             }
         }
         const bool open = (nib & (state == 1 ? DIR_FOPEN : DIR_EOPEN)) != 0;
@@ -166,10 +123,24 @@ __device__ TraceOut trace_walk(const uint32_t *__restrict__ dir, int n, int R, i
             --j;
         }
         if (open) state = 0;
+        return true;
     }
-    TraceOut o;
-    o.M = M; o.D = D; o.G = G; o.i0 = i; o.j0 = j;
-    return o;
+    __device__ __forceinline__ TraceOut out() const
+    {
+        TraceOut o;
+        o.M = M; o.D = D; o.G = G; o.i0 = i; o.j0 = j;
+        return o;
+    }
+};
+
+template <bool LOCAL, bool W16>
+__device__ __forceinline__ TraceOut trace_walk(const uint32_t *dir, int n, int R, int i, int j,
+                                               const uint8_t *V, const uint8_t *Hs, const int *ssm,
+                                               int go, int ge, int h)
+{
+    Walker<LOCAL, W16> w(dir, n, R, i, j, V, Hs, ssm, go, ge, h);
+    while (w.step()) {}
+    return w.out();
 }
 
 }  // namespace pg
