@@ -4,13 +4,8 @@
 // in the two halves of 32-bit registers: the low half works R rows, the high
 // half the R rows below them one column behind.  A warp is a wavefront of 64
 // virtual lanes (virtual lane v = 2 * lane + half works column k - v + 1 at
-// step k), and each packed max / add (PTX max.u16x2, add.s16x2) computes two
-// cells.  Values are held biased by 2^15 (v + 32768 in each half), so unsigned
-// order is signed order: max.u16x2 does the recurrence, and the difference
-// x - y of two values with x >= y (all that the decisions compare) is a plain
-// 32-bit subtraction that borrows nothing across the halves -- the compiler
-// may issue it on the FMA pipe, beside add.s16x2, while the ALU pipe bounds
-// the loop.  The high half's upper neighbour is the low half of the same lane one
+// step k), and each packed max / add (PTX max.s16x2, add.s16x2) computes two
+// cells.  The high half's upper neighbour is the low half of the same lane one
 // step earlier; the low half's is the high half of the lane above, handed down
 // by one __shfl_up_sync of the packed edge.
 //
@@ -21,8 +16,7 @@
 // steps).  Larger regions run on the 32-bit lanes of dp_warp_dir.
 //
 // Decisions come from equalities on the packed values, not from predicates:
-// min.u16x2(x - y, 1) is 1 in the halves where x > y, for x >= y.  Nibble of
-// cell (i, j):
+// min.u16x2(x ^ y, 1) is 1 in the halves where x != y.  Nibble of cell (i, j):
 //   bit 0   H is not the diagonal (diagonal wins every tie)
 //   bit 1   with bit 0: H is E (else F), under the tie policy's order of F and E
 //   bit 2   E(i, j) was opened from H(i, j-1)
@@ -52,26 +46,24 @@ constexpr int SENT16 = NCODES;                 // residue code of column -1 and 
 constexpr int NC16 = NCODES + 1;
 constexpr int PROF16_BYTES = 2 * NC16 * 32 * 8; // per warp: low and high halves' profiles
 constexpr uint32_t ONE2 = 0x00010001u;
-constexpr uint32_t ZERO2 = 0x80008000u;        // 0 in both halves, biased
-constexpr int BIAS16 = 32768;
 
+__device__ __forceinline__ uint32_t v16max(uint32_t a, uint32_t b)
+{
+    uint32_t d;
+    asm("max.s16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
 __device__ __forceinline__ uint32_t v16add(uint32_t a, uint32_t b)
 {
     uint32_t d;
     asm("add.s16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
     return d;
 }
-__device__ __forceinline__ uint32_t v16maxu(uint32_t a, uint32_t b)
+// 1 in each half where a != b, else 0
+__device__ __forceinline__ uint32_t v16ne(uint32_t a, uint32_t b)
 {
     uint32_t d;
-    asm("max.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
-    return d;
-}
-// for biased a >= b in both halves: 1 in each half where a > b, else 0
-__device__ __forceinline__ uint32_t v16gt(uint32_t a, uint32_t b)
-{
-    uint32_t d;
-    asm("min.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a - b), "r"(ONE2));
+    asm("min.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a ^ b), "r"(ONE2));
     return d;
 }
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t s)
@@ -86,9 +78,9 @@ __host__ __device__ __forceinline__ uint32_t pk16(int lo, int hi)
 }
 // a border value of the 32-bit helpers (whose sentinel is NEG = -2^30) in 16 bits
 __device__ __forceinline__ int c16(int x) { return x < NEG16 ? NEG16 : x; }
-// two values in biased form, and one half back as a value
-__host__ __device__ __forceinline__ uint32_t pkb(int lo, int hi) { return pk16(lo + BIAS16, hi + BIAS16); }
-__device__ __forceinline__ int halfb(uint32_t x, int h) { return (int)((x >> (16 * h)) & 0xffffu) - BIAS16; }
+__device__ __forceinline__ int lo16(uint32_t x) { return (int)(int16_t)(x & 0xffffu); }
+__device__ __forceinline__ int hi16(uint32_t x) { return (int)(int16_t)(x >> 16); }
+__device__ __forceinline__ int half16(uint32_t x, int h) { return h ? hi16(x) : lo16(x); }
 
 // largest m + n that runs on 16-bit lanes (0: none)
 __host__ __forceinline__ int dir16_limit(int maxabs)
@@ -177,15 +169,15 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int h0 = dir_col0<LOCAL>(min(i_base + r + 1, m), go, ge, gmax).h;
-            Hl[r] = pkb(h0, NEG16);
-            Al[r] = pkb(NEG16 + ge, NEG16);
-            Gl[r] = pkb(h0 + go, NEG16 + go);
+            Hl[r] = pk16(h0, NEG16);
+            Al[r] = pk16(NEG16 + ge, NEG16);
+            Gl[r] = pk16(h0 + go, NEG16 + go);
         }
         const EdgeD e_up = dir_col0<LOCAL>(min(i_base, m), go, ge, gmax);
         const EdgeD e_lo = dir_col0<LOCAL>(min(i_base + R, m), go, ge, gmax);
         const EdgeD e_hi = dir_col0<LOCAL>(min(i_base + 2 * R, m), go, ge, gmax);
-        uint32_t in_h = pkb(e_up.h, e_lo.h), in_a = pkb(c16(e_up.a), c16(e_lo.a));
-        uint32_t out_h = pkb(e_lo.h, e_hi.h), out_a = pkb(c16(e_lo.a), c16(e_hi.a));
+        uint32_t in_h = pk16(e_up.h, e_lo.h), in_a = pk16(c16(e_up.a), c16(e_lo.a));
+        uint32_t out_h = pk16(e_lo.h, e_hi.h), out_a = pk16(c16(e_lo.a), c16(e_hi.a));
         const uint32_t in_sel = lane == 0 ? 0x5410u : 0x5432u;
         // residues: the low half's column at this step, the high half's (one behind)
         int hc_lo = SENT16;
@@ -195,7 +187,7 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
             if (j1 >= 1 && j1 <= n) hc_next = (int)__ldg(Hs + j1 - 1);
         }
         uint2 *dstep = reinterpret_cast<uint2 *>(dir) + (uint64_t)stripe * (uint64_t)(n + 63) * 32u + lane;
-        uint32_t sbs = ZERO2, sbs_seen = ZERO2;
+        uint32_t sbs = 0, sbs_seen = 0;
         int sbp0 = 0, sbp1 = 0;
         const int nsteps = n + v_last;
         for (int k = 0; k < nsteps; ++k) {
@@ -209,7 +201,7 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
                 if (rb == 0) e = dir_row0<LOCAL>(j, go, ge, gmax);
                 else if (j <= n) e = bnd[j];
                 else { e.h = 0; e.a = NEG16; }
-                th = (uint32_t)(c16(e.h) + BIAS16); ta = (uint32_t)(c16(e.a) + BIAS16);
+                th = (uint32_t)c16(e.h); ta = (uint32_t)c16(e.a);
             }
             in_h = prmt(th, out_h, in_sel);
             in_a = prmt(ta, out_a, in_sel);
@@ -228,18 +220,15 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     const uint32_t s2 = prmt(r < 4 ? pl.x : pl.y, r < 4 ? ph.x : ph.y, sx_sel(r & 3));
-                    const uint32_t E = v16maxu(Al[r], Gl[r]);
-                    const uint32_t pe = OPEN_FIRST ? (v16gt(E, Gl[r]) ^ ONE2) : v16gt(E, Al[r]);
-                    // the local floor goes on the diagonal term: max(dg, 0, E, F) is
-                    // H, and a cell whose H is 0 ends the walk whatever its bits say
-                    uint32_t dg = v16add(dH, s2);
-                    if (LOCAL) dg = v16maxu(dg, ZERO2);
-                    const uint32_t X = v16maxu(dg, E);
-                    const uint32_t F = v16maxu(cA, cG);
-                    const uint32_t pf = OPEN_FIRST ? (v16gt(F, cG) ^ ONE2) : v16gt(F, cA);
-                    const uint32_t Hv = v16maxu(X, F);
-                    const uint32_t nd = v16gt(Hv, dg);
-                    const uint32_t ne = E_FIRST ? (v16gt(Hv, E) ^ ONE2) : v16gt(Hv, F);
+                    const uint32_t E = v16max(Al[r], Gl[r]);
+                    const uint32_t pe = OPEN_FIRST ? (v16ne(E, Gl[r]) ^ ONE2) : v16ne(E, Al[r]);
+                    const uint32_t dg = v16add(dH, s2);
+                    const uint32_t X = v16max(dg, E);
+                    const uint32_t F = v16max(cA, cG);
+                    const uint32_t pf = OPEN_FIRST ? (v16ne(F, cG) ^ ONE2) : v16ne(F, cA);
+                    const uint32_t Hv = LOCAL ? __vimax_s16x2_relu(X, F) : v16max(X, F);
+                    const uint32_t nd = v16ne(Hv, dg);
+                    const uint32_t ne = E_FIRST ? (v16ne(Hv, E) ^ ONE2) : v16ne(Hv, F);
                     const uint32_t nib = nd + 2u * ne + 4u * pe + 8u * pf;
                     if (r < 4) W0 += nib << (4 * (r & 3));
                     else W1 += nib << (4 * (r & 3));
@@ -250,7 +239,7 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
                     Hl[r] = Hv;
                     Al[r] = v16add(E, ge2);
                     Gl[r] = G;
-                    if (LOCAL) sbs = v16maxu(sbs, Hv);
+                    if (LOCAL) sbs = v16max(sbs, Hv);
                 }
                 dstep[(uint64_t)k * 32u] = make_uint2(prmt(W0, W1, 0x5410u), prmt(W0, W1, 0x7632u));
                 out_h = Hl[R - 1];
@@ -260,8 +249,8 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
                     const int jb = j - h;
                     if (jb >= 1 && jb <= n) {
                         EdgeD e;
-                        e.h = halfb(out_h, h);
-                        e.a = halfb(out_a, h);
+                        e.h = half16(out_h, h);
+                        e.a = half16(out_a, h);
                         bnd[jb] = e;
                     }
                 }
@@ -269,12 +258,12 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
                     // a new maximum in this column: its first row
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
-                        const int s = halfb(sbs, h);
-                        if (s != halfb(sbs_seen, h)) {
+                        const int s = half16(sbs, h);
+                        if (s != half16(sbs_seen, h)) {
                             int rr = R - 1;
 #pragma unroll
                             for (int r = R - 1; r >= 0; --r)
-                                if (halfb(Hl[r], h) == s) rr = r;
+                                if (half16(Hl[r], h) == s) rr = r;
                             const int p = ((j - h) << 3) | rr;
                             if (h) sbp1 = p; else sbp0 = p;
                         }
@@ -289,7 +278,7 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
             // half, and against earlier stripes a tie goes to the smaller column
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int s = halfb(sbs, h);
+                const int s = half16(sbs, h);
                 const int sp = h ? sbp1 : sbp0;
                 const int sj = sp >> 3;
                 if (s > 0 && (s > bs || (s == bs && sj < bj))) {
@@ -303,7 +292,7 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
             int hs = 0;
 #pragma unroll
             for (int r = 0; r < R; ++r)
-                if (r == rl) hs = halfb(Hl[r], h);
+                if (r == rl) hs = half16(Hl[r], h);
             res.score = __shfl_sync(FULL, hs, t_last);
         }
     }
