@@ -14,9 +14,7 @@
 // or at a cell whose H fell to 0, and starts at that cell.
 //
 // One thread walks one region, one 4-byte direction word per step (the
-// words sit in HBM: the DP of a whole chunk writes them first); each step
-// also prefetches into L2 the word that a diagonal walk reaches a few steps
-// later.  Two
+// words sit in HBM: the DP of a whole chunk writes them first).  Two
 // read-ahead schemes measured slower and were dropped: a per-thread tile of
 // 8 steps x 4 lanes (a refill somewhere in the warp at nearly every step,
 // and 8 sectors read per refill), and one warp per region reading 32-step x
@@ -45,14 +43,12 @@ struct TraceOut {
 template <bool LOCAL, bool W16>
 struct Walker {
     static constexpr int VL = W16 ? 64 : 32;
-    static constexpr int PF = 4;   // prefetch distance in diagonal steps
     const uint32_t *dir;
     const uint8_t *V, *Hs;
     const int *ssm;
     int n, R, go, ge;
     int i, j, h;
     int s = 0, v = 0, r = 0;   // row i - 1 as stripe, lane, row of the lane (kept in step with i)
-    uint32_t inv = 0;          // ceil(2^16 / R): t / R = (t * inv) >> 16 for t < VL * R <= 512
     int state = 0;             // 0: H, 1: F (vertical gap), 2: E (horizontal gap)
     int last = 0;              // previous move: 0 diagonal / none, 1 vertical, 2 horizontal
     uint32_t M = 0, D = 0, G = 0;
@@ -63,7 +59,6 @@ struct Walker {
                                       int go_, int ge_, int h_)
         : dir(dir_), V(V_), Hs(Hs_), ssm(ssm_), n(n_), R(R_), go(go_), ge(ge_), i(i_), j(j_), h(h_)
     {
-        inv = (0x10000u + (uint32_t)R - 1u) / (uint32_t)R;
         if (i > 0) {
             const int r0 = i - 1, rows = VL * R;
             s = r0 / rows;
@@ -92,15 +87,6 @@ struct Walker {
         }
         if (W16 && LOCAL && state == 0 && h == 0) { done = true; return false; }
         const uint32_t w = __ldg(dir + ((uint64_t)s * (uint64_t)(n + VL - 1) + (uint64_t)(j - 1 + v)) * VL + v);
-        // the word the walk needs PF diagonal steps from here, fetched into L2
-        // now (no register waits on it): most moves are diagonal
-        if (i > PF && j > PF) {
-            int t = v * R + r - PF, sp = s;
-            if (t < 0) { t += VL * R; --sp; }
-            const int vp = (int)(((uint32_t)t * inv) >> 16);
-            const uint32_t *a = dir + ((uint64_t)sp * (uint64_t)(n + VL - 1) + (uint64_t)(j - 1 - PF + vp)) * VL + vp;
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
-        }
         const uint32_t nib = (w >> (4 * r)) & 15u;
         if (state == 0) {
             bool diag;
