@@ -557,6 +557,9 @@ def run_manytomany(args, rank, world, local_rank):
     ctx = capi.Context(cfg)
     ctx.set_seqs(0, w.ascii, w.offs)
     ctx.share_row_seqs()
+    if args.set_tuning:
+        ctx.set_tuning(**{k: int(v) for k, v in
+                          (kv.split("=") for kv in args.set_tuning.split(","))})
     stream = torch.cuda.Stream(device=dev)
     torch.cuda.set_stream(stream)
     nb = args.blocks
