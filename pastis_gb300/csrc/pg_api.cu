@@ -475,7 +475,11 @@ static int run_dir(pg_ctx *c, const pg::KParams &kp, uint64_t n, int grid, cudaS
         cudaFree(c->d_dir);
         c->d_dir = nullptr; c->dir_cap = 0;
     }
-    const uint64_t want = std::max<uint64_t>(16, std::min<uint64_t>(total, budget));
+    // grow at least twofold (up to the cap): a stream of batches of growing
+    // need reallocates a few times, not once per batch
+    const uint64_t need = std::max<uint64_t>(16, std::min<uint64_t>(total, budget));
+    const uint64_t want = need > c->dir_cap ? std::min<uint64_t>(budget, std::max<uint64_t>(need, 2 * c->dir_cap))
+                                            : need;
     if (want > c->dir_cap) {
         cudaFree(c->d_dir);
         c->d_dir = nullptr; c->dir_cap = 0;

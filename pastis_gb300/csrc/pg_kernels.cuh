@@ -218,15 +218,11 @@ constexpr int NBUCKET = 24;
 constexpr int SCHED_WORDS = 2 * NBUCKET;
 constexpr int BUCKET_NONE = 23;   // no DP work
 
-// Regions of at most this many rows stay on 32-bit lanes in the traceback
-// form: on 16-bit lanes a region of m <= 64 rows fills only m / 2 lanes (one
-// row per virtual lane) and still pays the 64-lane wavefront ramp.
-constexpr int DIR16_MIN_ROWS = 64;
-
-// traceback form: 16-bit lanes for this region (pg_dpdir16.cuh)?
+// traceback form: 16-bit lanes for this region (pg_dpdir16.cuh)?  (Keeping
+// regions of up to 64 or 128 rows on 32-bit lanes measured no faster.)
 __host__ __device__ __forceinline__ bool dir16_use(const KParams &kp, int m, int n)
 {
-    return m > DIR16_MIN_ROWS && n > 0 && m + n <= kp.dir16_lim;
+    return m > 0 && n > 0 && m + n <= kp.dir16_lim;
 }
 
 // traceback form: rows per lane of the region's DP, 16-bit lanes (12..19) after 32-bit (4..11)
