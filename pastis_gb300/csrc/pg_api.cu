@@ -310,7 +310,7 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     if (cfg->mode == PG_MODE_XDROP) {
         CUD(pg::stat_occupancy(true, &per_sm));
         int px = 0, pw = 0;
-        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&px, pg::k_xd, pg::XT, 0));
+        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&px, pg::k_xdf, pg::XT, 0));
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pw, pg::k_xd_wide, pg::WARPS * 32, 0));
         c->grid_xd = c->nsm * std::max(px, 1);
         c->grid_wide = c->nsm * std::max(pw, 1);
@@ -574,7 +574,7 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
             xmax = std::min<uint64_t>(xmax, (uint64_t)c->nsm * (uint64_t)c->tune.xd_blocks_per_sm);
         const int gx = (int)std::min<uint64_t>(xmax, need_xd);
         if (c->tune.xd_int16 && c->cfg.xdrop <= pg::XMAX16) pg::k_xd16<<<gx, pg::XT, 0, st>>>(kp);
-        else pg::k_xd<<<gx, pg::XT, 0, st>>>(kp);
+        else pg::k_xdf<<<gx, pg::XT, 0, st>>>(kp);
         pg::k_xd_wide<<<c->grid_wide, blk, 0, st>>>(kp);
         if (kp.order) {
             pg::k_hist<true><<<gsched, 256, 0, st>>>(kp);

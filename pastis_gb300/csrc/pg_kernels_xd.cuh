@@ -69,6 +69,129 @@ __global__ void __launch_bounds__(XT) k_xd(const KParams kp)
     if (exec) atomicAdd(kp.exec_cells, exec);
 }
 
+// ------------------------------------------------------------------ k_xdf
+// k_xd with each thread stepping one extension direction at a time: when a
+// direction ends the thread starts the next one at once (the task's other
+// direction, or the next task) instead of waiting, as k_xd's threads do, for
+// the longest extension in the warp.  The next tasks' inputs are read ahead
+// in three stages (work counter, pair record, sequence offsets), each
+// consumed a task later, so starting a task waits on no memory.  Results,
+// overflow list and cell counts are k_xd's.
+struct XfTask {
+    uint64_t t;          // task: pair t >> 1, seed t & 1
+    pg_pair pr;
+    uint64_t r0, r1, c0, c1;
+    int valid, idx_ok;
+};
+
+__global__ void __launch_bounds__(XT) k_xdf(const KParams kp)
+{
+    __shared__ int ssm[32 * 32];
+    __shared__ int ring[3 * XW * XT];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
+    int *base = ring + threadIdx.x;
+    const uint64_t ntask = 2 * kp.n;
+    unsigned long long exec = 0;
+    // read-ahead pipeline: a (task id), b (+ pair record), c (+ offsets)
+    XfTask a, b, c;
+    auto fetch_id = [&](XfTask &x) {
+        x.t = atomicAdd(&kp.counter[1], 1u);
+        x.valid = x.t < ntask;
+    };
+    auto fetch_pair = [&](XfTask &x) {
+        if (x.valid) x.pr = kp.pairs[x.t >> 1];
+    };
+    auto fetch_offs = [&](XfTask &x) {
+        x.idx_ok = 0;
+        if (!x.valid) return;
+        const uint64_t r = (uint64_t)x.pr.row + kp.roff, cc = (uint64_t)x.pr.col + kp.coff;
+        if (r >= kp.nr || cc >= kp.nc) return;
+        x.idx_ok = 1;
+        x.r0 = kp.roffs[r]; x.r1 = kp.roffs[r + 1];
+        x.c0 = kp.coffs[cc]; x.c1 = kp.coffs[cc + 1];
+    };
+    fetch_id(c); fetch_pair(c); fetch_offs(c);
+    fetch_id(b); fetch_pair(b);
+    fetch_id(a);
+
+    XdDir<XW, XT> dir;
+    XdRec rec{0, 0, 0, 0, 0u, 0u};
+    uint64_t task = 0;
+    const uint8_t *V = nullptr, *Hs = nullptr;
+    int m = 0, n = 0, bv = 0, ev = 0, bh = 0, eh = 0;
+    int phase = 0;     // 0: start a task, 1: left direction running, 2: right direction running
+    auto write_rec = [&]() {
+        if (rec.flags & XF_OVF) {
+            rec.cells = 0;
+            const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
+            kp.ovf[slot] = (uint32_t)task;
+        } else if (!(rec.flags & (XF_NONE | XF_SAME | XF_BADIDX))) {
+            rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev;
+            rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
+            exec += rec.cells;
+        }
+        kp.xd[task] = rec;
+    };
+    for (;;) {
+        while (phase == 0) {
+            if (!c.valid) break;
+            // take c, move the pipeline on by one task
+            const XfTask cur = c;
+            c = b; fetch_offs(c);
+            b = a; fetch_pair(b);
+            fetch_id(a);
+            task = cur.t;
+            const int s = (int)(task & 1);
+            const pg_pair &pr = cur.pr;
+            rec = XdRec{0, 0, 0, 0, 0u, 0u};
+            if (!cur.idx_ok) {
+                rec.flags = XF_BADIDX;
+            } else if (s >= kp.seed_count ||
+                       (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
+                rec.flags = XF_NONE;
+            } else if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
+                rec.flags = XF_SAME;
+            } else {
+                V = kp.rseq + cur.r0; m = (int)(cur.r1 - cur.r0);
+                Hs = kp.cseq + cur.c0; n = (int)(cur.c1 - cur.c0);
+                if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
+                if (bv > 0 && bh > 0) {
+                    dir.init(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1, kp.xg, kp.xdrop, base);
+                    phase = 1;
+                } else if (ev < m && eh < n) {
+                    dir.init(V + ev, m - ev, 1, Hs + eh, n - eh, 1, kp.xg, kp.xdrop, base);
+                    phase = 2;
+                }
+            }
+            if (phase == 0) write_rec();
+        }
+        if (phase == 0) break;          // no task left for this thread
+        if (dir.step(ssm, kp.xg, kp.xdrop, base)) continue;
+        const XdOut x = dir.finish(base);
+        rec.cells += x.cells;
+        if (!x.ok) {
+            rec.flags |= XF_OVF;
+            write_rec();
+            phase = 0;
+        } else if (phase == 1) {
+            bv -= x.dv; bh -= x.dh;
+            if (ev < m && eh < n) {
+                dir.init(V + ev, m - ev, 1, Hs + eh, n - eh, 1, kp.xg, kp.xdrop, base);
+                phase = 2;
+            } else {
+                write_rec();
+                phase = 0;
+            }
+        } else {
+            ev += x.dv; eh += x.dh;
+            write_rec();
+            phase = 0;
+        }
+    }
+    if (exec) atomicAdd(kp.exec_cells, exec);
+}
+
 // ------------------------------------------------------------- k_xd_wide
 __device__ __forceinline__ XdOut xdrop_dir_any(const uint8_t *V, int nv, int vstep,
                                                const uint8_t *Hs, int nh, int hstep,

@@ -213,6 +213,100 @@ __device__ __forceinline__ XdOut xdrop_dir_thread(const uint8_t *__restrict__ V,
     return o;
 }
 
+// xdrop_dir_thread cut at anti-diagonal bounds so that a caller can step
+// one extension direction at a time and start another the moment one ends
+// (k_xdf).  init sets up a direction of at least one residue on each side;
+// step computes one anti-diagonal and returns whether the direction goes on
+// (false also on ring overflow, ok = 0); finish gives its end point.  The
+// results equal xdrop_dir_thread's step for step.
+template <int W, int NT>
+struct XdDir {
+    const uint8_t *V, *Hs;
+    int vstep, hstep, cols, rows;
+    int k1, k2, k3, off1, len1, off2, len2, off3, len3;
+    int best, d, lo, hi, ok;
+    uint32_t cells;
+
+#define XRING(k, c) base[((k) * W + ((c) & (W - 1))) * NT]
+    __device__ __forceinline__ void init(const uint8_t *V_, int nv, int vstep_, const uint8_t *Hs_, int nh,
+                                         int hstep_, int g, int X, int *base)
+    {
+        V = V_; Hs = Hs_; vstep = vstep_; hstep = hstep_;
+        cols = nv + 1; rows = nh + 1;
+        k1 = 0; k2 = 1; k3 = 2;
+        off1 = 0; len1 = 0; off2 = 0; len2 = 1; off3 = 0; len3 = 2;
+        XRING(k2, 0) = 0;
+        const int v1 = (-g > X) ? UND : g;
+        XRING(k3, 0) = v1;
+        XRING(k3, 1) = v1;
+        best = 0; d = 1; lo = 1; hi = 2; ok = 1; cells = 0;
+    }
+    __device__ __forceinline__ bool step(const int *__restrict__ ssm, int g, int X, int *base)
+    {
+        ++d;
+        const int kt = k1; k1 = k2; k2 = k3; k3 = kt;
+        off1 = off2; len1 = len2;
+        off2 = off3; len2 = len3;
+        off3 = lo - 1; len3 = hi + 1 - off3;
+        if (len3 > W) { ok = 0; return false; }
+        const int thr = best - X;
+        {
+            const int bval = (d * g > best - X) ? d * g : UND;
+            XRING(k3, off3) = (off3 == 0) ? bval : UND;
+            XRING(k3, hi) = (d == hi && hi < cols) ? bval : UND;
+        }
+        int dbest = d * g;
+        int a2prev = XRING(k2, lo - 1);
+        const uint8_t *vp = V + vstep * (lo - 1);
+        const uint8_t *hp = Hs + hstep * (d - lo - 1);
+        for (int c = lo; c < hi; ++c) {
+            const int a2c = XRING(k2, c);
+            int v = max(a2prev, a2c) + g;
+            const int dg = XRING(k1, c - 1) + ssm[(int)__ldg(vp) * 32 + (int)__ldg(hp)];
+            v = max(v, dg);
+            const bool live = v >= thr;
+            XRING(k3, c) = live ? v : UND;
+            if (live) dbest = max(dbest, v);
+            a2prev = a2c;
+            vp += vstep;
+            hp -= hstep;
+        }
+        if (dbest > best) best = dbest;
+        cells += (uint32_t)(hi - lo);
+        while (lo - off3 < len3 && XRING(k3, lo) == UND && lo - off2 - 1 < len2 && XRING(k2, lo - 1) == UND)
+            ++lo;
+        while (hi - off3 > 0 && XRING(k3, hi - 1) == UND && XRING(k2, hi - 1) == UND)
+            --hi;
+        ++hi;
+        if (lo < d + 2 - rows) lo = d + 2 - rows;
+        if (hi > cols) hi = cols;
+        return lo < hi;
+    }
+    __device__ __forceinline__ XdOut finish(const int *base) const
+    {
+        XdOut o{0, 0, cells, ok};
+        if (!ok) return o;
+        int lc = off3 + len3 - 2, lr = d - lc, ls = XRING(k3, lc);
+        if (ls == UND) {
+            const int ca = off2 + len2 - 2;
+            if (XRING(k2, ca) != UND) {
+                lc = ca; lr = d - 1 - lc; ls = XRING(k2, ca);
+            } else if (len2 > 2 && XRING(k2, ca - 1) != UND) {
+                lc = ca - 1; lr = d - 1 - lc; ls = XRING(k2, ca - 1);
+            }
+        }
+        if (ls == UND) {
+            for (int k = 0; k < len1; ++k) {
+                const int val = XRING(k1, off1 + k);
+                if (val > ls) { ls = val; lc = off1 + k; lr = d - 2 - lc; }
+            }
+        }
+        if (ls != UND) { o.dv = lc; o.dh = lr; }
+        return o;
+    }
+#undef XRING
+};
+
 // ------------------------------------------------------------------------
 // The per-thread extension in 16-bit lanes, two band cells per instruction
 // (__vmaxs2 / __vaddss2 / __vcmpges2 on int16x2).  A live cell lies in
