@@ -170,7 +170,7 @@ int pg_last_launches(const pg_ctx *ctx);
  * timing candidates on a sample of the caller's own batch. */
 typedef struct pg_tuning {
     int32_t dp_blocks_per_sm;   /* k_ga / k_sw resident blocks per SM; 0 = occupancy limit */
-    int32_t xd_blocks_per_sm;   /* k_xd resident blocks per SM; 0 = occupancy limit        */
+    int32_t xd_blocks_per_sm;   /* k_xdf resident blocks per SM; 0 = occupancy limit       */
     int32_t bucket_order;       /* 1: pairs in DP-bucket order, tallest first; 0: input order */
     int32_t rows_max;           /* cap on DP rows per lane, 1..8 (wide statistics stop at 4) */
     int32_t graph;              /* 1: pg_align / pg_align_device capture the batch's launches

@@ -2,7 +2,7 @@
 
 The choices it makes never change a result, only how fast a batch runs:
 resident blocks per SM of the DP kernels (k_ga / k_sw) and of the X-drop
-extension (k_xd), the bucketed pair order, 16-bit lanes for the X-drop
+extension (k_xdf), the bucketed pair order, 16-bit lanes for the X-drop
 extension, the traceback form of the alignment DP, and CUDA-graph replay of
 the batch's launches.
 Candidates are timed with the library's own CUDA events (pg_kernel_ms) on a

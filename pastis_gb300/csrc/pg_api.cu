@@ -118,7 +118,7 @@ struct pg_ctx {
     cudaStream_t stream = nullptr;
     int nsm = 0;
     int grid = 0;                  // persistent blocks of the warp-per-pair kernel
-    int grid_xd = 0;               // persistent blocks of k_xd
+    int grid_xd = 0;               // persistent blocks of k_xdf
     int grid_wide = 0;             // blocks of k_xd_wide
     Side side[2];
     bool cols_share_rows = false;

@@ -1,14 +1,16 @@
 // pg_kernels.cuh -- batch kernels behind pg_align (sm_103a).
 //
 // --sxa (X-drop), five launches per batch:
-//   k_xd       one thread per (pair, seed): both X-drop directions on a
+//   k_xdf      one thread per (pair, seed): both X-drop directions on a
 //              16-slot per-thread ring in shared memory (the band of the
-//              default gap model never spans more than 13 columns); threads
-//              take the next (pair, seed) from a device counter, so long and
-//              short extensions balance.  Writes the extended region.
+//              default gap model, with its two border columns, never spans more
+//              than 15 columns), stepped
+//              one direction at a time; threads take the next (pair, seed)
+//              from a device counter the moment a direction ends, so long
+//              and short extensions balance.  Writes the extended region.
 //   k_xd_wide  one warp per (pair, seed) whose band outgrew the thread ring:
 //              256-slot shared ring, per-warp global ring beyond that.
-//              (k_xd16, the 16-bit-lane form of k_xd, is a tuning option.)
+//              (k_xd16, a 16-bit-lane form of the extension, is a tuning option.)
 //   k_hist, k_bucket  the bucket order of the pairs for k_ga (schedule below).
 //   k_ga       one warp per pair: global alignment with statistics over each
 //              seed's region (a region equal to the first seed's is not
@@ -36,8 +38,8 @@ namespace pg {
 
 constexpr int WARPS = 8;          // warps per block (k_ga, k_sw, k_xd_wide)
 constexpr int RING_W = 256;       // shared ring per warp in k_xd_wide
-constexpr int XT = 128;           // threads per block in k_xd
-constexpr int XW = 16;            // per-thread ring slots in k_xd
+constexpr int XT = 128;           // threads per block in k_xdf / k_xd16
+constexpr int XW = 16;            // per-thread ring slots in k_xdf
 
 // status word bits (read back by the host after a batch)
 constexpr int ST_BAD_INDEX = 1;
@@ -66,7 +68,7 @@ struct KParams {
     const int8_t *sm;             // 25 x 25
     int go, ge, xg, xdrop, seed_len, seed_count, flags, ani_thr;
     double cov_thr;
-    unsigned int *counter;        // [0] k_ga / k_sw pairs, [1] k_xd tasks, [2] overflow count
+    unsigned int *counter;        // [0] k_ga / k_sw pairs, [1] k_xdf tasks, [2] overflow count
     int *status;                  // error bits
     unsigned long long *exec_cells; // cells actually computed: [0] X-drop bands, [1] DP
     XdRec *xd;                    // 2 per pair

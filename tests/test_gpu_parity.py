@@ -43,7 +43,7 @@ def run_both(mode, w, cfg, O, pairs=None, roff=0, coff=0, share=True):
     else:
         ctx.set_seqs(1, ascii_, w.offs)
     got = ctx.align(pairs, roff, coff)
-    # traceback form by default: X-drop: k_xd, k_xd_wide, k_hist, k_bucket,
+    # traceback form by default: X-drop: k_xdf, k_xd_wide, k_hist, k_bucket,
     # k_dirsize, k_ga_dir, k_tb_ga; SW: k_hist, k_bucket, k_dirsize, k_sw_dir, k_tb_sw
     assert ctx.last_launches() == (7 if mode == capi.MODE_XDROP else 5)
     codes = O.encode(bytes(ascii_))
