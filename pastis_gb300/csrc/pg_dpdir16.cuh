@@ -196,10 +196,15 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
             const uint32_t dgH = in_h;
             const int j = k - 2 * lane + 1;              // low half's column; high half: j - 1
             uint32_t th = rh, ta = ra;
-            if (lane == 0) {
+            if (rb == 0) {
+                // row 0 (lane 0 is at column j >= 1): computed by every lane and
+                // selected, no branch on the lane
+                const int b0 = LOCAL ? 0 : c16(go + (j - 1) * gmax);
+                th = lane == 0 ? (uint32_t)b0 : rh;
+                ta = lane == 0 ? (uint32_t)NEG16 : ra;
+            } else if (lane == 0) {
                 EdgeD e;
-                if (rb == 0) e = dir_row0<LOCAL>(j, go, ge, gmax);
-                else if (j <= n) e = bnd[j];
+                if (j <= n) e = bnd[j];
                 else { e.h = 0; e.a = NEG16; }
                 th = (uint32_t)c16(e.h); ta = (uint32_t)c16(e.a);
             }

@@ -21,11 +21,12 @@ namespace pg {
 // consumed a task later, so starting a task waits on no memory.  A band
 // wider than the 16-slot ring sends the task to the overflow list for
 // k_xd_wide.
-struct XfTask {
-    uint64_t t;          // task: pair t >> 1, seed t & 1
-    pg_pair pr;
+// a task in the read-ahead pipeline: id, then its pair record, then what
+// starting it needs (flags, its seed, its sequences' offsets)
+constexpr uint32_t XFT_VALID = 1, XFT_IDX = 2, XFT_SAME = 4, XFT_FEW = 8;
+struct XfReady {
+    uint32_t t, flags, seed;   // seed: rs | cs << 16 of the task's seed
     uint64_t r0, r1, c0, c1;
-    int valid, idx_ok;
 };
 
 __global__ void __launch_bounds__(XT) k_xdf(const KParams kp)
@@ -35,33 +36,43 @@ __global__ void __launch_bounds__(XT) k_xdf(const KParams kp)
     load_sm(ssm, kp.sm);
     __syncthreads();
     int *base = ring + threadIdx.x;
-    const uint64_t ntask = 2 * kp.n;
+    const uint32_t ntask = (uint32_t)(2 * kp.n);
     unsigned long long exec = 0;
-    // read-ahead pipeline: a (task id), b (+ pair record), c (+ offsets)
-    XfTask a, b, c;
-    auto fetch_id = [&](XfTask &x) {
-        x.t = atomicAdd(&kp.counter[1], 1u);
-        x.valid = x.t < ntask;
+    // read-ahead pipeline: ta (task id), tb + pb (pair record), c (ready)
+    uint32_t ta, tb;
+    pg_pair pb;
+    XfReady c;
+    auto load_pair = [&](uint32_t t, pg_pair &pr) {
+        if (t < ntask) pr = kp.pairs[t >> 1];
     };
-    auto fetch_pair = [&](XfTask &x) {
-        if (x.valid) x.pr = kp.pairs[x.t >> 1];
-    };
-    auto fetch_offs = [&](XfTask &x) {
-        x.idx_ok = 0;
-        if (!x.valid) return;
-        const uint64_t r = (uint64_t)x.pr.row + kp.roff, cc = (uint64_t)x.pr.col + kp.coff;
+    auto make_ready = [&](uint32_t t, const pg_pair &pr, XfReady &x) {
+        x.t = t;
+        x.flags = 0;
+        if (t >= ntask) return;
+        x.flags = XFT_VALID;
+        const uint64_t r = (uint64_t)pr.row + kp.roff, cc = (uint64_t)pr.col + kp.coff;
+        const int s = (int)(t & 1);
+        x.seed = s ? ((uint32_t)pr.rs1 | ((uint32_t)pr.cs1 << 16)) : ((uint32_t)pr.rs0 | ((uint32_t)pr.cs0 << 16));
+        if (pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) x.flags |= XFT_SAME;
+        if (pr.count < 2) x.flags |= XFT_FEW;
         if (r >= kp.nr || cc >= kp.nc) return;
-        x.idx_ok = 1;
+        x.flags |= XFT_IDX;
         x.r0 = kp.roffs[r]; x.r1 = kp.roffs[r + 1];
         x.c0 = kp.coffs[cc]; x.c1 = kp.coffs[cc + 1];
     };
-    fetch_id(c); fetch_pair(c); fetch_offs(c);
-    fetch_id(b); fetch_pair(b);
-    fetch_id(a);
+    {
+        const uint32_t t0 = atomicAdd(&kp.counter[1], 1u);
+        pg_pair p0;
+        load_pair(t0, p0);
+        make_ready(t0, p0, c);
+        tb = atomicAdd(&kp.counter[1], 1u);
+        load_pair(tb, pb);
+        ta = atomicAdd(&kp.counter[1], 1u);
+    }
 
     XdDir<XW, XT> dir;
     XdRec rec{0, 0, 0, 0, 0u, 0u};
-    uint64_t task = 0;
+    uint32_t task = 0;
     const uint8_t *V = nullptr, *Hs = nullptr;
     int m = 0, n = 0, bv = 0, ev = 0, bh = 0, eh = 0;
     int phase = 0;     // 0: start a task, 1: left direction running, 2: right direction running
@@ -69,7 +80,7 @@ __global__ void __launch_bounds__(XT) k_xdf(const KParams kp)
         if (rec.flags & XF_OVF) {
             rec.cells = 0;
             const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
-            kp.ovf[slot] = (uint32_t)task;
+            kp.ovf[slot] = task;
         } else if (!(rec.flags & (XF_NONE | XF_SAME | XF_BADIDX))) {
             rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev;
             rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
@@ -79,27 +90,33 @@ __global__ void __launch_bounds__(XT) k_xdf(const KParams kp)
     };
     for (;;) {
         while (phase == 0) {
-            if (!c.valid) break;
+            if (!(c.flags & XFT_VALID)) break;
             // take c, move the pipeline on by one task
-            const XfTask cur = c;
-            c = b; fetch_offs(c);
-            b = a; fetch_pair(b);
-            fetch_id(a);
+            const XfReady cur = c;
+            make_ready(tb, pb, c);
+            tb = ta;
+            load_pair(tb, pb);
+            ta = atomicAdd(&kp.counter[1], 1u);
             task = cur.t;
             const int s = (int)(task & 1);
-            const pg_pair &pr = cur.pr;
             rec = XdRec{0, 0, 0, 0, 0u, 0u};
-            if (!cur.idx_ok) {
+            if (!(cur.flags & XFT_IDX)) {
                 rec.flags = XF_BADIDX;
             } else if (s >= kp.seed_count ||
-                       (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
+                       (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && (cur.flags & XFT_FEW))) {
                 rec.flags = XF_NONE;
-            } else if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
+            } else if (s == 1 && (cur.flags & XFT_SAME)) {
                 rec.flags = XF_SAME;
             } else {
                 V = kp.rseq + cur.r0; m = (int)(cur.r1 - cur.r0);
                 Hs = kp.cseq + cur.c0; n = (int)(cur.c1 - cur.c0);
-                if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
+                // seed_region for the task's seed
+                bv = (int)(cur.seed & 0xffffu); bh = (int)(cur.seed >> 16);
+                ev = bv + kp.seed_len; eh = bh + kp.seed_len;
+                if (ev > m || eh > n) {
+                    bv = min(bv, m); ev = min(ev, m); bh = min(bh, n); eh = min(eh, n);
+                    rec.flags |= XF_BAD;
+                }
                 if (bv > 0 && bh > 0) {
                     dir.init(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1, kp.xg, kp.xdrop, base);
                     phase = 1;

@@ -146,6 +146,7 @@ struct XdDir {
     int k1, k2, k3, off1, len1, off2, len2, off3, len3;
     int best, d, lo, hi, ok;
     uint32_t cells;
+    int vr0, hr0;        // residues of the band's first cell on the next anti-diagonal
 
 #define XRING(k, c) base[((k) * W + ((c) & (W - 1))) * NT]
     __device__ __forceinline__ void init(const uint8_t *V_, int nv, int vstep_, const uint8_t *Hs_, int nh,
@@ -160,6 +161,8 @@ struct XdDir {
         XRING(k3, 0) = v1;
         XRING(k3, 1) = v1;
         best = 0; d = 1; lo = 1; hi = 2; ok = 1; cells = 0;
+        vr0 = __ldg(V);                 // anti-diagonal 2 starts at column 1, row 1
+        hr0 = __ldg(Hs);
     }
     __device__ __forceinline__ bool step(const int *__restrict__ ssm, int g, int X, int *base)
     {
@@ -179,17 +182,22 @@ struct XdDir {
         int a2prev = XRING(k2, lo - 1);
         const uint8_t *vp = V + vstep * (lo - 1);
         const uint8_t *hp = Hs + hstep * (d - lo - 1);
+        // residues are read one cell ahead (and the first cell's a step ahead)
+        int vr = vr0, hr = hr0;
         for (int c = lo; c < hi; ++c) {
+            vp += vstep;
+            hp -= hstep;
+            int vn = 0, hn = 0;
+            if (c + 1 < hi) { vn = __ldg(vp); hn = __ldg(hp); }
             const int a2c = XRING(k2, c);
             int v = max(a2prev, a2c) + g;
-            const int dg = XRING(k1, c - 1) + ssm[(int)__ldg(vp) * 32 + (int)__ldg(hp)];
+            const int dg = XRING(k1, c - 1) + ssm[vr * 32 + hr];
             v = max(v, dg);
             const bool live = v >= thr;
             XRING(k3, c) = live ? v : UND;
             if (live) dbest = max(dbest, v);
             a2prev = a2c;
-            vp += vstep;
-            hp -= hstep;
+            vr = vn; hr = hn;
         }
         if (dbest > best) best = dbest;
         cells += (uint32_t)(hi - lo);
@@ -200,6 +208,11 @@ struct XdDir {
         ++hi;
         if (lo < d + 2 - rows) lo = d + 2 - rows;
         if (hi > cols) hi = cols;
+        if (lo < hi) {
+            // the next anti-diagonal (d + 1) starts at column lo: V[lo - 1], H[d - lo]
+            vr0 = __ldg(V + vstep * (lo - 1));
+            hr0 = __ldg(Hs + hstep * (d - lo));
+        }
         return lo < hi;
     }
     __device__ __forceinline__ XdOut finish(const int *base) const
