@@ -170,7 +170,7 @@ int pg_last_launches(const pg_ctx *ctx);
  * timing candidates on a sample of the caller's own batch. */
 typedef struct pg_tuning {
     int32_t dp_blocks_per_sm;   /* k_ga / k_sw resident blocks per SM; 0 = occupancy limit */
-    int32_t xd_blocks_per_sm;   /* k_xdf resident blocks per SM; 0 = occupancy limit       */
+    int32_t xd_blocks_per_sm;   /* X-drop extension resident blocks per SM; 0 = occupancy limit */
     int32_t bucket_order;       /* 1: pairs in DP-bucket order, tallest first; 0: input order */
     int32_t rows_max;           /* cap on DP rows per lane, 1..8 (wide statistics stop at 4) */
     int32_t graph;              /* 1: pg_align / pg_align_device capture the batch's launches
@@ -187,7 +187,14 @@ typedef struct pg_tuning {
                                    ((m + n + 4) * largest |score| <= 30000), 32-bit lanes for
                                    the rest; no graph capture in either form */
     int32_t dir_arena_mb;       /* cap on that arena in MiB; 0 = a third of the device memory */
-} pg_tuning;                    /* 32 bytes */
+    int32_t xd_stepped;         /* X-drop extension, a thread per (pair, seed): 1 steps one
+                                   extension direction at a time and starts the next the
+                                   moment one ends; 0 runs each task to its end (fewer
+                                   registers, more resident warps); -1 picks 1 while the
+                                   resident sequences fit half of L2, else 0 (measured:
+                                   1 faster with sequences in L2, 0 when they stream
+                                   from DRAM) */
+} pg_tuning;                    /* 36 bytes */
 
 /* The built-in tuning.  A new context starts from it with dp_traceback = 2
  * (measured fastest in both modes); with a score table whose magnitudes pass

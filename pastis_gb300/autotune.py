@@ -1,10 +1,10 @@
 """Autotuner for the batch launch shape (pg_tuning).
 
 The choices it makes never change a result, only how fast a batch runs:
-resident blocks per SM of the DP kernels (k_ga / k_sw) and of the X-drop
-extension (k_xdf), the bucketed pair order, 16-bit lanes for the X-drop
-extension, the traceback form of the alignment DP, and CUDA-graph replay of
-the batch's launches.
+resident blocks per SM of the DP kernels and of the X-drop extension, the
+form of the X-drop extension (a direction per step, or each task run to its
+end), the bucketed pair order, the form of the alignment DP, and CUDA-graph
+replay of the batch's launches.
 Candidates are timed with the library's own CUDA events (pg_kernel_ms) on a
 batch the caller supplies,
 normally a sample of the real one, and the winner is cached in a JSON file
@@ -26,7 +26,7 @@ GRID = {
     "dp_blocks_per_sm": (1, 0),      # 0 = occupancy limit (2 on GB300)
     "xd_blocks_per_sm": (4, 0),      # 0 = occupancy limit (7 on GB300)
     "bucket_order": (1, 0),
-    "xd_int16": (0, 1),
+    "xd_stepped": (1, 0),            # X-drop extension: a direction per step, or run to end
     "dp_traceback": (2, 0),          # 2 = traceback form on 16-bit lanes, 0 = statistics
 }
 
@@ -117,7 +117,7 @@ def tune(ctx, run, key=None, device=0, reps=3, grid=None, use_cache=True, log=No
               "candidates": len(rows), "validated_on_full_batch": validated, "default_ms": next(
                   (m for m, c in rows if c == {"dp_blocks_per_sm": 0, "xd_blocks_per_sm": 0,
                                                "bucket_order": 1, "graph": 0,
-                                               "xd_int16": 0, "dp_traceback": 2}),
+                                               "xd_stepped": 1, "dp_traceback": 2}),
                   None)}
     if entry:
         try:

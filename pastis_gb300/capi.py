@@ -73,10 +73,11 @@ class Tuning(ctypes.Structure):
     _fields_ = [("dp_blocks_per_sm", ctypes.c_int32), ("xd_blocks_per_sm", ctypes.c_int32),
                 ("bucket_order", ctypes.c_int32), ("rows_max", ctypes.c_int32),
                 ("graph", ctypes.c_int32), ("xd_int16", ctypes.c_int32),
-                ("dp_traceback", ctypes.c_int32), ("dir_arena_mb", ctypes.c_int32)]
+                ("dp_traceback", ctypes.c_int32), ("dir_arena_mb", ctypes.c_int32),
+                ("xd_stepped", ctypes.c_int32)]
 
     FIELDS = ("dp_blocks_per_sm", "xd_blocks_per_sm", "bucket_order", "rows_max", "graph",
-              "xd_int16", "dp_traceback", "dir_arena_mb")
+              "xd_int16", "dp_traceback", "dir_arena_mb", "xd_stepped")
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k in self.FIELDS}

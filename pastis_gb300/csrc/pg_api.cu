@@ -98,6 +98,7 @@ struct Side {
     uint8_t *seq = nullptr;
     uint64_t *offs = nullptr;
     uint64_t n = 0;
+    uint64_t nres = 0;      // residues of all its sequences
     uint32_t maxlen = 0;
 };
 
@@ -119,6 +120,8 @@ struct pg_ctx {
     int nsm = 0;
     int grid = 0;                  // persistent blocks of the warp-per-pair kernel
     int grid_xd = 0;               // persistent blocks of k_xdf
+    int grid_xd_run = 0;           // persistent blocks of k_xd
+    uint64_t l2_bytes = 0;         // the device's L2 cache
     int grid_wide = 0;             // blocks of k_xd_wide
     Side side[2];
     bool cols_share_rows = false;
@@ -298,6 +301,11 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     CUD(cudaMemset(c->d_exec, 0, 2 * sizeof(unsigned long long)));
     for (int k = 0; k < 3; ++k) CUD(cudaEventCreate(&c->ev[k]));
     CUD(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, cfg->device));
+    {
+        int l2 = 0;
+        CUD(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, cfg->device));
+        c->l2_bytes = (uint64_t)l2;
+    }
     CUD(pg::stat_set_attributes());
     CUD(pg::dir_set_attributes());
     {
@@ -311,6 +319,9 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
         CUD(pg::stat_occupancy(true, &per_sm));
         int px = 0, pw = 0;
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&px, pg::k_xdf, pg::XT, 0));
+        int pr = 0;
+        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pr, pg::k_xd, pg::XT, 0));
+        c->grid_xd_run = c->nsm * std::max(pr, 1);
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pw, pg::k_xd_wide, pg::WARPS * 32, 0));
         c->grid_xd = c->nsm * std::max(px, 1);
         c->grid_wide = c->nsm * std::max(pw, 1);
@@ -426,6 +437,7 @@ int pg_set_seqs(pg_ctx *c, int32_t side, const char *residues, const uint64_t *o
         return fail(e4 == cudaErrorMemoryAllocation ? PG_ERR_OOM : PG_ERR_CUDA, "pg_set_seqs: %s", cudaGetErrorString(e4));
     }
     s.n = n;
+    s.nres = total;
     s.maxlen = maxlen;
     ++c->epoch;
     return ensure_scratch(c);
@@ -568,13 +580,20 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
     const int gsched = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (n + 255) / 256);
     CU(record_event(c, c->ev[0], st));
     if (c->cfg.mode == PG_MODE_XDROP) {
+        // extension kernel: k_xdf (a direction per step, the next task read
+        // ahead) while the resident sequences fit half of L2; k_xd (each task
+        // run to its end, more resident warps) when residues stream from DRAM
+        const uint64_t nres = c->side[0].nres + (c->cols_share_rows ? 0 : c->side[1].nres);
+        const bool stepped = c->tune.xd_stepped >= 0 ? c->tune.xd_stepped != 0 : nres <= c->l2_bytes / 2;
+        const bool int16 = c->tune.xd_int16 && c->cfg.xdrop <= pg::XMAX16;
         const uint64_t need_xd = (2 * n + pg::XT - 1) / pg::XT;
-        uint64_t xmax = (uint64_t)c->grid_xd;
+        uint64_t xmax = (uint64_t)((stepped && !int16) ? c->grid_xd : c->grid_xd_run);
         if (c->tune.xd_blocks_per_sm > 0)
             xmax = std::min<uint64_t>(xmax, (uint64_t)c->nsm * (uint64_t)c->tune.xd_blocks_per_sm);
         const int gx = (int)std::min<uint64_t>(xmax, need_xd);
-        if (c->tune.xd_int16 && c->cfg.xdrop <= pg::XMAX16) pg::k_xd16<<<gx, pg::XT, 0, st>>>(kp);
-        else pg::k_xdf<<<gx, pg::XT, 0, st>>>(kp);
+        if (int16) pg::k_xd16<<<gx, pg::XT, 0, st>>>(kp);
+        else if (stepped) pg::k_xdf<<<gx, pg::XT, 0, st>>>(kp);
+        else pg::k_xd<<<gx, pg::XT, 0, st>>>(kp);
         pg::k_xd_wide<<<c->grid_wide, blk, 0, st>>>(kp);
         if (kp.order) {
             pg::k_hist<true><<<gsched, 256, 0, st>>>(kp);
@@ -722,6 +741,7 @@ void pg_tuning_default(pg_tuning *t)
     t->xd_int16 = 0;
     t->dp_traceback = 0;
     t->dir_arena_mb = 0;
+    t->xd_stepped = -1;
 }
 
 int pg_get_tuning(const pg_ctx *c, pg_tuning *out)
@@ -744,6 +764,7 @@ int pg_set_tuning(pg_ctx *c, const pg_tuning *t)
     if (t->xd_int16 != 0 && t->xd_int16 != 1) return fail(PG_ERR_ARG, "xd_int16 must be 0 or 1");
     if (t->dp_traceback < 0 || t->dp_traceback > 2) return fail(PG_ERR_ARG, "dp_traceback must be 0, 1 or 2");
     if (t->dir_arena_mb < 0) return fail(PG_ERR_ARG, "dir_arena_mb must be >= 0");
+    if (t->xd_stepped < -1 || t->xd_stepped > 1) return fail(PG_ERR_ARG, "xd_stepped must be -1, 0 or 1");
     c->tune = *t;
     ++c->epoch;                         // launch shapes changed: recapture
     return PG_OK;
@@ -789,6 +810,7 @@ int pg_internal_adopt_side(pg_ctx *c, int side, uint8_t *d_codes, uint64_t *d_of
     s.offs = d_offs;
     s.n = n;
     s.maxlen = maxlen;
+    if (n > 0) CU(cudaMemcpy(&s.nres, d_offs + n, sizeof s.nres, cudaMemcpyDeviceToHost));
     ++c->epoch;
     return ensure_scratch(c);
 }

@@ -1,8 +1,9 @@
 // pg_kernels_xd.cuh -- the X-drop extension kernels (one definition: only
-// pg_api.cu includes this file): k_xdf, thread per (pair, seed) task with the
-// 32-bit band (pg_xdrop.cuh), one direction stepped at a time; k_xd16, a
-// thread per task on 16-bit lanes (tuning option xd_int16); k_xd_wide, warp
-// per task for the bands that overflow a thread's ring.
+// pg_api.cu includes this file): k_xdf and k_xd, thread per (pair, seed) task
+// with the 32-bit band (pg_xdrop.cuh), stepping one direction at a time or
+// running each task to its end (tuning option xd_stepped); k_xd16, a thread
+// per task on 16-bit lanes (tuning option xd_int16); k_xd_wide, warp per task
+// for the bands that overflow a thread's ring.
 #pragma once
 #include <cstdint>
 
@@ -10,13 +11,77 @@
 
 namespace pg {
 
+// ------------------------------------------------------------------ k_xd
+// One thread per (pair, seed) task, run to its end before the thread takes
+// the next: fewer registers than k_xdf (7 resident blocks per SM against 5),
+// which wins when the residues stream from DRAM (sequence sets larger than
+// L2); a warp waits on its longest extension.
+__global__ void __launch_bounds__(XT) k_xd(const KParams kp)
+{
+    __shared__ int ssm[32 * 32];
+    __shared__ int ring[3 * XW * XT];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
+    int *base = ring + threadIdx.x;
+    const uint64_t ntask = 2 * kp.n;
+    unsigned long long exec = 0;
+    for (;;) {
+        const uint64_t task = atomicAdd(&kp.counter[1], 1u);
+        if (task >= ntask) break;
+        const uint64_t p = task >> 1;
+        const int s = (int)(task & 1);
+        const pg_pair pr = kp.pairs[p];
+        XdRec rec{0, 0, 0, 0, 0u, 0u};
+        const uint8_t *V, *Hs;
+        int m, n;
+        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
+            rec.flags = XF_BADIDX;
+        } else if (s >= kp.seed_count ||
+                   (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
+            rec.flags = XF_NONE;
+        } else if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
+            rec.flags = XF_SAME;
+        } else {
+            int bv, ev, bh, eh;
+            if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
+            bool ok = true;
+            if (bv > 0 && bh > 0) {
+                const XdOut x = xdrop_dir_thread<XW, XT>(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1,
+                                                         ssm, kp.xg, kp.xdrop, base);
+                ok = x.ok;
+                rec.cells += x.cells;
+                bv -= x.dv; bh -= x.dh;
+            }
+            if (ok && ev < m && eh < n) {
+                const XdOut x = xdrop_dir_thread<XW, XT>(V + ev, m - ev, 1, Hs + eh, n - eh, 1,
+                                                         ssm, kp.xg, kp.xdrop, base);
+                ok = x.ok;
+                rec.cells += x.cells;
+                ev += x.dv; eh += x.dh;
+            }
+            if (ok) {
+                rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev;
+                rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
+                exec += rec.cells;
+            } else {
+                rec.flags |= XF_OVF;
+                rec.cells = 0;
+                const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
+                kp.ovf[slot] = (uint32_t)task;
+            }
+        }
+        kp.xd[task] = rec;
+    }
+    if (exec) atomicAdd(kp.exec_cells, exec);
+}
+
 // ------------------------------------------------------------------ k_xdf
 // One thread per (pair, seed) task, each thread stepping one extension
 // direction at a time: when a direction ends the thread starts the next one
 // at once (the task's other direction, or the next task).  Running each task
 // to its end before taking the next, as an earlier kernel did, left a warp
 // waiting on its longest extension: 6.5 of 32 lanes active per instruction,
-// 28.6 ms per 1M pairs against 19.2 ms here.  The next tasks' inputs are read ahead
+// 28.6 ms per 1M pairs against 16.8 ms here (xdrop1m, sequences in L2).  The next tasks' inputs are read ahead
 // in three stages (work counter, pair record, sequence offsets), each
 // consumed a task later, so starting a task waits on no memory.  A band
 // wider than the 16-slot ring sends the task to the overflow list for

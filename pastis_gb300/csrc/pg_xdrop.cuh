@@ -131,11 +131,92 @@ __device__ inline XdOut xdrop_dir_warp(const uint8_t *__restrict__ V, int nv, in
     return o;
 }
 
-// The same extension run by one thread, cut at anti-diagonal bounds so that
-// a caller can step one direction at a time and start another the moment one
-// ends (k_xdf).  The ring holds W ints per anti-diagonal; slot (array k,
-// column c) sits at base[(k*W + (c & (W-1))) * NT] where base = ring +
-// threadIdx.x, so the 32 lanes of a warp always touch 32 different banks.
+// The same extension run by one thread from start to end (k_xd).  The ring
+// holds W ints per
+// anti-diagonal; slot (array k, column c) sits at base[(k*W + (c & (W-1))) * NT]
+// where base = ring + threadIdx.x, so the 32 lanes of a warp always touch 32
+// different banks.  Bands wider than W report overflow (ok = 0).
+template <int W, int NT>
+__device__ __forceinline__ XdOut xdrop_dir_thread(const uint8_t *__restrict__ V, int nv, int vstep,
+                                                  const uint8_t *__restrict__ Hs, int nh, int hstep,
+                                                  const int *__restrict__ ssm, int g, int X,
+                                                  int *__restrict__ base)
+{
+    XdOut o{0, 0, 0u, 1};
+    const int cols = nv + 1, rows = nh + 1;
+    if (cols == 1 || rows == 1) return o;
+#define RING(k, c) base[((k) * W + ((c) & (W - 1))) * NT]
+    int k1 = 0, k2 = 1, k3 = 2;
+    int off1 = 0, len1 = 0, off2 = 0, len2 = 1, off3 = 0, len3 = 2;
+    RING(k2, 0) = 0;
+    {
+        const int v1 = (-g > X) ? UND : g;
+        RING(k3, 0) = v1;
+        RING(k3, 1) = v1;
+    }
+    int best = 0, d = 1, lo = 1, hi = 2;
+    while (lo < hi) {
+        ++d;
+        const int kt = k1; k1 = k2; k2 = k3; k3 = kt;
+        off1 = off2; len1 = len2;
+        off2 = off3; len2 = len3;
+        off3 = lo - 1; len3 = hi + 1 - off3;
+        if (len3 > W) { o.ok = 0; return o; }
+        const int thr = best - X;
+        {
+            const int bval = (d * g > best - X) ? d * g : UND;
+            RING(k3, off3) = (off3 == 0) ? bval : UND;
+            RING(k3, hi) = (d == hi && hi < cols) ? bval : UND;
+        }
+        int dbest = d * g;
+        int a2prev = RING(k2, lo - 1);
+        const uint8_t *vp = V + vstep * (lo - 1);
+        const uint8_t *hp = Hs + hstep * (d - lo - 1);
+        for (int c = lo; c < hi; ++c) {
+            const int a2c = RING(k2, c);
+            int v = max(a2prev, a2c) + g;
+            const int dg = RING(k1, c - 1) + ssm[(int)__ldg(vp) * 32 + (int)__ldg(hp)];
+            v = max(v, dg);
+            const bool live = v >= thr;
+            RING(k3, c) = live ? v : UND;
+            if (live) dbest = max(dbest, v);
+            a2prev = a2c;
+            vp += vstep;
+            hp -= hstep;
+        }
+        if (dbest > best) best = dbest;
+        o.cells += (uint32_t)(hi - lo);
+        while (lo - off3 < len3 && RING(k3, lo) == UND && lo - off2 - 1 < len2 && RING(k2, lo - 1) == UND)
+            ++lo;
+        while (hi - off3 > 0 && RING(k3, hi - 1) == UND && RING(k2, hi - 1) == UND)
+            --hi;
+        ++hi;
+        if (lo < d + 2 - rows) lo = d + 2 - rows;
+        if (hi > cols) hi = cols;
+    }
+    int lc = off3 + len3 - 2, lr = d - lc, ls = RING(k3, lc);
+    if (ls == UND) {
+        const int ca = off2 + len2 - 2;
+        if (RING(k2, ca) != UND) {
+            lc = ca; lr = d - 1 - lc; ls = RING(k2, ca);
+        } else if (len2 > 2 && RING(k2, ca - 1) != UND) {
+            lc = ca - 1; lr = d - 1 - lc; ls = RING(k2, ca - 1);
+        }
+    }
+    if (ls == UND) {
+        for (int k = 0; k < len1; ++k) {
+            const int val = RING(k1, off1 + k);
+            if (val > ls) { ls = val; lc = off1 + k; lr = d - 2 - lc; }
+        }
+    }
+#undef RING
+    if (ls != UND) { o.dv = lc; o.dh = lr; }
+    return o;
+}
+
+// xdrop_dir_thread cut at anti-diagonal bounds so that a caller can step one
+// direction at a time and start another the moment one ends (k_xdf), on the
+// same ring.
 // init sets up a direction of at least one residue on each side; step
 // computes one anti-diagonal and returns whether the direction goes on (false
 // also when the band outgrows the ring: ok = 0); finish gives its end point.

@@ -40,7 +40,7 @@ def test_struct_layouts(native):
     assert capi.PAIR_DTYPE == oracle.PAIR_DTYPE
     assert capi.RESULT_DTYPE == oracle.RESULT_DTYPE
     assert ctypes.sizeof(capi.Config) == 64
-    assert ctypes.sizeof(capi.Tuning) == 32
+    assert ctypes.sizeof(capi.Tuning) == 36
 
 
 def test_tuning_defaults_without_gpu(native):
@@ -50,7 +50,7 @@ def test_tuning_defaults_without_gpu(native):
     t = capi.default_tuning()
     assert t.as_dict() == {"dp_blocks_per_sm": 0, "xd_blocks_per_sm": 0, "bucket_order": 1,
                            "rows_max": 8, "graph": 0, "xd_int16": 0, "dp_traceback": 0,
-                           "dir_arena_mb": 0}
+                           "dir_arena_mb": 0, "xd_stepped": -1}
 
 
 def test_defaults_and_errors_without_gpu(native):
