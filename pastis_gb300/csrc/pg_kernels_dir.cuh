@@ -193,7 +193,9 @@ __device__ __forceinline__ void walk_both(const KParams &kp, const uint32_t *con
 }
 
 // traceback and result of the tasks [t0, t1), one thread per task: the same
-// record k_ga writes
+// record k_ga writes.  Five resident blocks per SM (48 registers, a few
+// spilled) measured 1 % faster than four: the walks wait on memory, so more
+// of them in flight count for more than the spills.
 __global__ void __launch_bounds__(256, 5) k_tb_ga(const KParams kp, uint64_t t0, uint64_t t1,
                                                const uint64_t *doff, const uint8_t *arena,
                                                const int *dsc)
@@ -337,7 +339,7 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint
 
 // traceback and result of the tasks [t0, t1), one thread per task: the same
 // record k_sw writes
-__global__ void __launch_bounds__(256, 6) k_tb_sw(const KParams kp, uint64_t t0, uint64_t t1,
+__global__ void __launch_bounds__(256) k_tb_sw(const KParams kp, uint64_t t0, uint64_t t1,
                                                const uint64_t *doff, const uint8_t *arena,
                                                const int *dsc)
 {
