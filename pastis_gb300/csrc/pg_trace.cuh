@@ -85,8 +85,10 @@ struct Walker {
             done = true;
             return false;
         }
-        if (W16 && LOCAL && state == 0 && h == 0) { done = true; return false; }
+        // the word of (i, j) first (i, j >= 1 here): its load does not wait on h,
+        // whose substitution-score lookups it overlaps
         const uint32_t w = __ldg(dir + ((uint64_t)s * (uint64_t)(n + VL - 1) + (uint64_t)(j - 1 + v)) * VL + v);
+        if (W16 && LOCAL && state == 0 && h == 0) { done = true; return false; }
         const uint32_t nib = (w >> (4 * r)) & 15u;
         if (state == 0) {
             bool diag;
