@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC]
-CUDA_UNITS = ("pg_api.cu", "pg_stat.cu", "pg_dir.cu", "pg_filter.cu", "pg_kmer.cu", "pg_fasta.cu")
+CUDA_UNITS = ("pg_api.cu", "pg_stat.cu", "pg_dir.cu", "pg_dir_ga.cu", "pg_dir_sw.cu", "pg_filter.cu", "pg_kmer.cu", "pg_fasta.cu")
 
 
 def _steps():

@@ -470,17 +470,21 @@ static int run_dir(pg_ctx *c, const pg::KParams &kp, uint64_t n, int grid, cudaS
         CU(cudaMalloc(&c->d_dbytes, (n + 1) * sizeof(uint64_t)));
         CU(cudaMalloc(&c->d_doff, (n + 1) * sizeof(uint64_t)));
         CU(cudaMalloc(&c->d_dsc, n * 4 * sizeof(int)));
-        CU(cudaMalloc(&c->d_t1, sizeof(uint64_t)));
+        CU(cudaMalloc(&c->d_t1, 2 * sizeof(uint64_t)));   // chunk end, checked regions
         CU(cub::DeviceScan::ExclusiveSum(nullptr, c->scan_bytes, c->d_dbytes, c->d_doff, n + 1));
         CU(cudaMalloc(&c->d_scan, c->scan_bytes));
         c->dirb_cap = n + 1;
     }
     const int gs = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (n + 256) / 256);
-    pg::dir_sizes(xdrop, kp, c->d_dbytes, gs, st);
+    unsigned long long *d_nchk = reinterpret_cast<unsigned long long *>(c->d_t1 + 1);
+    CU(cudaMemsetAsync(d_nchk, 0, sizeof *d_nchk, st));
+    pg::dir_sizes(xdrop, kp, c->d_dbytes, d_nchk, gs, st);
     size_t sb = c->scan_bytes;
     CU(cub::DeviceScan::ExclusiveSum(c->d_scan, sb, c->d_dbytes, c->d_doff, n + 1, st));
     uint64_t total = 0;
+    unsigned long long nchk = 0;
     CU(cudaMemcpyAsync(&total, c->d_doff + n, sizeof total, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&nchk, d_nchk, sizeof nchk, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     const uint64_t budget = c->tune.dir_arena_mb > 0 ? ((uint64_t)c->tune.dir_arena_mb << 20) : c->dir_budget;
     if (c->dir_cap > budget) {           // a smaller cap than the arena held so far
@@ -525,12 +529,11 @@ static int run_dir(pg_ctx *c, const pg::KParams &kp, uint64_t n, int grid, cudaS
         const uint64_t nt = t1 - t0;
         const int g = (int)std::min<uint64_t>((uint64_t)grid, (nt + pg::WARPS - 1) / pg::WARPS);
         const int gt = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (nt + 255) / 256);
-        pg::dir_run(xdrop, tie, kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc, g, dyn, gt, st);
+        launches += pg::dir_run(xdrop, tie, kp, t0, t1, c->d_doff, c->d_dir, c->d_dsc, g, dyn, gt, nchk > 0, st);
         CU(cudaGetLastError());
-        launches += 2;
         t0 = t1;
     }
-    return launches;   // k_dirsize, then per chunk (k_chunk_end,) the DP and the traceback
+    return launches;   // k_dirsize, then per chunk (k_chunk_end,) the DP (and its checked pass) and the traceback
 }
 
 // The batch timing events.  Inside a stream capture they become external
@@ -569,6 +572,14 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
     kp.rows_cap = c->tune.rows_max;
     kp.dir = c->tune.dp_traceback ? 1 : 0;
     kp.dir16_lim = c->tune.dp_traceback == 2 ? c->lim16 : 0;
+    // regions past dir16_lim run the checked 16-bit form while their borders fit:
+    // local borders are 0, global ones go + (i - 1) * max(go, ge) >= -30000
+    kp.dir16_side = 0;
+    if (kp.dir16_lim > 0) {
+        const int gmax = std::max(c->go, c->ge);
+        if (c->cfg.mode == PG_MODE_SW || gmax >= 0) kp.dir16_side = 65535;
+        else kp.dir16_side = std::min(65535, (pg::SAT16_DP - std::abs(c->go)) / -gmax);
+    }
     CU(cudaMemsetAsync(c->d_counter, 0, (4 + pg::SCHED_WORDS) * sizeof(unsigned int), st));
     CU(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
     const uint64_t need_blocks = (n + pg::WARPS - 1) / pg::WARPS;

@@ -73,6 +73,7 @@ struct DirOut {
     int score;
     int ei, ej;     // local: first maximum in column-major order
     int have;
+    int sat = 0;    // 16-bit lanes, checked form: a value left [-30000, 30000]
 };
 
 template <int TIE, int R, bool LOCAL>

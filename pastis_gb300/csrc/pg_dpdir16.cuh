@@ -9,11 +9,13 @@
 // step earlier; the low half's is the high half of the lane above, handed down
 // by one __shfl_up_sync of the packed edge.
 //
-// Scores are exact while every value of the region stays inside int16: a
-// region runs here only when (m + n + 4) * maxabs <= 30000, maxabs the largest
-// magnitude among the substitution scores and the two gap scores
-// (dir16_limit), which bounds every H, E, F and their sums (a path of m + n
-// steps).  Larger regions run on the 32-bit lanes of dp_warp_dir.
+// Scores are exact while every value of the region stays inside int16.  A
+// region with (m + n + 4) * maxabs <= 30000, maxabs the largest magnitude
+// among the substitution scores and the two gap scores (dir16_limit), has
+// every H, E, F and their sums bounded there (a path of m + n steps).  A
+// larger region whose borders still fit runs the checked form (CHECK below)
+// and is redone on the 32-bit lanes of dp_warp_dir if a value leaves the
+// range; the rest run on 32-bit lanes from the start.
 //
 // Decisions come from equalities on the packed values, not from predicates:
 // min.u16x2(x ^ y, 1) is 1 in the halves where x != y.  Nibble of cell (i, j):
@@ -51,6 +53,12 @@ __device__ __forceinline__ uint32_t v16max(uint32_t a, uint32_t b)
 {
     uint32_t d;
     asm("max.s16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+__device__ __forceinline__ uint32_t v16min(uint32_t a, uint32_t b)
+{
+    uint32_t d;
+    asm("min.s16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
     return d;
 }
 __device__ __forceinline__ uint32_t v16add(uint32_t a, uint32_t b)
@@ -112,7 +120,16 @@ __device__ __forceinline__ constexpr uint32_t sx_sel(int q)
            ((uint32_t)((4 + q) | 8) << 12);
 }
 
-template <int TIE, int R, bool LOCAL>
+// CHECK: the region is beyond the size that bounds every value inside int16
+// (its borders still fit): the kernel tracks the least and the greatest H of
+// each half (local: the greatest, which its best cell tracking keeps anyway)
+// and reports sat when one left [-30000, 30000].  H moves by at most the
+// largest score magnitude from a neighbour, so the first value to leave the
+// range is still exact and no wrapped value goes unseen; the caller then
+// redoes the region on 32-bit lanes.
+constexpr int SAT16_DP = 30000;
+
+template <int TIE, int R, bool LOCAL, bool CHECK = false>
 __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
                                 const uint8_t *__restrict__ Hs, int n,
                                 const int *__restrict__ ssm, uint2 *__restrict__ prof,
@@ -128,6 +145,7 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
     int bs = 0, bi = 0, bj = 0;
     DirOut res;
     res.have = 0; res.ei = 0; res.ej = 0; res.score = 0;
+    uint32_t hmn = pk16(0, 0), hmx = pk16(0, 0), lmx = pk16(0, 0);   // CHECK: extremes of H
     for (int rb = 0, stripe = 0; rb < m; rb += 64 * R, ++stripe) {
         const int rows_here = min(64 * R, m - rb);
         const int v_last = (rows_here - 1) / R;
@@ -245,6 +263,7 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
                     Al[r] = v16add(E, ge2);
                     Gl[r] = G;
                     if (LOCAL) sbs = v16max(sbs, Hv);
+                    if (CHECK && !LOCAL) { hmn = v16min(hmn, Hv); hmx = v16max(hmx, Hv); }
                 }
                 dstep[(uint64_t)k * 32u] = make_uint2(prmt(W0, W1, 0x5410u), prmt(W0, W1, 0x7632u));
                 out_h = Hl[R - 1];
@@ -278,6 +297,7 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
             }
         }
         __syncwarp();
+        if (CHECK && LOCAL) lmx = v16max(lmx, sbs);
         if (LOCAL) {
             // the low half's rows come before the high half's: a tie keeps the low
             // half, and against earlier stripes a tie goes to the smaller column
@@ -313,6 +333,12 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
         res.score = bs;
         res.have = bs > 0;
         res.ei = bi; res.ej = bj;
+    }
+    if (CHECK) {
+        const uint32_t mx = LOCAL ? lmx : hmx;
+        const bool out = lo16(mx) > SAT16_DP || hi16(mx) > SAT16_DP ||
+                         (!LOCAL && (lo16(hmn) < -SAT16_DP || hi16(hmn) < -SAT16_DP));
+        res.sat = __any_sync(FULL, out) ? 1 : 0;
     }
     return res;
 }

@@ -82,6 +82,7 @@ struct KParams {
     int rows_cap = 8;                // cap on DP rows per lane (tuning)
     int dir = 0;                     // 1: the traceback form (pg_kernels_dir.cuh) runs the DP
     int dir16_lim = 0;               // traceback form: regions with m + n <= this on 16-bit lanes
+    int dir16_side = 0;              // ... and larger ones with both sides <= this, checked
 };
 
 __device__ __forceinline__ void load_sm(int *ssm, const int8_t *sm)
@@ -220,11 +221,19 @@ constexpr int NBUCKET = 24;
 constexpr int SCHED_WORDS = 2 * NBUCKET;
 constexpr int BUCKET_NONE = 23;   // no DP work
 
-// traceback form: 16-bit lanes for this region (pg_dpdir16.cuh)?  (Keeping
-// regions of up to 64 or 128 rows on 32-bit lanes measured no faster.)
+// traceback form, lanes of a region's DP (pg_dpdir16.cuh): 0 32-bit; 1 16-bit,
+// every value provably inside int16; 2 16-bit, checked, redone on 32-bit lanes
+// if a value leaves the range (its borders fit: both sides <= dir16_side).
+// (Keeping regions of up to 64 or 128 rows on 32-bit lanes measured no faster.)
+__host__ __device__ __forceinline__ int dir16_mode(const KParams &kp, int m, int n)
+{
+    if (m <= 0 || n <= 0 || kp.dir16_lim <= 0) return 0;
+    if (m + n <= kp.dir16_lim) return 1;
+    return (m <= kp.dir16_side && n <= kp.dir16_side) ? 2 : 0;
+}
 __host__ __device__ __forceinline__ bool dir16_use(const KParams &kp, int m, int n)
 {
-    return m > 0 && n > 0 && m + n <= kp.dir16_lim;
+    return dir16_mode(kp, m, n) != 0;
 }
 
 // traceback form: rows per lane of the region's DP, 16-bit lanes (12..19) after 32-bit (4..11)

@@ -39,16 +39,22 @@ __device__ __forceinline__ SeedPlan seed_plan(const KParams &kp, uint64_t p)
     return sp;
 }
 
-// direction bytes of an m x n region: 16-bit lanes where it fits, else 32-bit
+// direction bytes of an m x n region: 16-bit lanes where they run, 32-bit
+// otherwise, room for either where a checked region may be redone
 __device__ __forceinline__ uint64_t region_bytes(const KParams &kp, int m, int n)
 {
-    if (dir16_use(kp, m, n)) return dir16_bytes(m, n, dir16_rows(m, kp.rows_cap));
-    return dir_bytes(m, n, dir_rows(m, kp.rows_cap));
+    const int mode = dir16_mode(kp, m, n);
+    const uint64_t b16 = mode ? dir16_bytes(m, n, dir16_rows(m, kp.rows_cap)) : 0;
+    const uint64_t b32 = mode != 1 ? dir_bytes(m, n, dir_rows(m, kp.rows_cap)) : 0;
+    return b16 > b32 ? b16 : b32;
 }
 
-__device__ __forceinline__ uint64_t region_dir_bytes(const KParams &kp, const XdRec &r)
+// a region's DP ran on 16-bit lanes (mode, and for a checked region the
+// redo flag its DP recorded)
+__device__ __forceinline__ bool region16(const KParams &kp, int m, int n, int redone)
 {
-    return region_bytes(kp, r.ev - r.bv, r.eh - r.bh);
+    const int mode = dir16_mode(kp, m, n);
+    return mode == 1 || (mode == 2 && !redone);
 }
 
 // this warp's score profile in the dynamic shared memory of the traceback DP
@@ -59,9 +65,12 @@ __device__ __forceinline__ uint2 *dir_prof(const KParams &kp)
 }
 
 // direction bytes of each task (bucket position t)
+// direction bytes of each task (bucket position t); *nchk += the checked
+// regions (mode 2) among them
 template <bool XDROP>
-__global__ void k_dirsize(const KParams kp, uint64_t *bytes)
+__global__ void k_dirsize(const KParams kp, uint64_t *bytes, unsigned long long *nchk)
 {
+    unsigned long long chk = 0;
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t <= kp.n;
          t += (uint64_t)gridDim.x * blockDim.x) {
         if (t == kp.n) { bytes[t] = 0; continue; }
@@ -70,22 +79,31 @@ __global__ void k_dirsize(const KParams kp, uint64_t *bytes)
         if (p < kp.n) {
             if (XDROP) {
                 const SeedPlan sp = seed_plan(kp, p);
-                if (sp.dp[0]) b += region_dir_bytes(kp, sp.rec[0]);
-                if (sp.dp[1]) b += region_dir_bytes(kp, sp.rec[1]);
+#pragma unroll
+                for (int s = 0; s < 2; ++s) {
+                    if (!sp.dp[s]) continue;
+                    const int rm = sp.rec[s].ev - sp.rec[s].bv, rn = sp.rec[s].eh - sp.rec[s].bh;
+                    b += region_bytes(kp, rm, rn);
+                    chk += dir16_mode(kp, rm, rn) == 2;
+                }
             } else {
                 const pg_pair pr = kp.pairs[p];
                 const uint8_t *V, *Hs;
                 int m, n;
-                if (pair_seqs(kp, pr, V, m, Hs, n)) b = region_bytes(kp, m, n);
+                if (pair_seqs(kp, pr, V, m, Hs, n)) {
+                    b = region_bytes(kp, m, n);
+                    chk += dir16_mode(kp, m, n) == 2;
+                }
             }
         }
         bytes[t] = b;
     }
+    if (chk) atomicAdd(nchk, chk);
 }
 
 // end of the chunk that starts at task t0: the largest t1 <= n with
 // doff[t1] - doff[t0] <= budget, at least t0 + 1
-__global__ void k_chunk_end(const uint64_t *doff, uint64_t t0, uint64_t n, uint64_t budget,
+static __global__ void k_chunk_end(const uint64_t *doff, uint64_t t0, uint64_t n, uint64_t budget,
                             uint64_t *t1)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -99,41 +117,54 @@ __global__ void k_chunk_end(const uint64_t *doff, uint64_t t0, uint64_t n, uint6
     *t1 = lo;
 }
 
-template <int TIE, bool LOCAL>
+// The DP of one region.  CHK false: a region on 16-bit lanes with every value
+// provably in range (mode 1) or on 32-bit lanes (mode 0); CHK true: a checked
+// region (mode 2), the checked 16-bit form and, if a value left the range, the
+// 32-bit form after it (sat = 1: the traceback walks the 32-bit layout).  The
+// kernels take checked regions in a pass of their own, so the common pass's
+// code stays free of the checked form.
+template <int TIE, bool LOCAL, bool CHK>
 __device__ __forceinline__ DirOut dp_dispatch_dir(const KParams &kp, const uint8_t *V, int m,
                                                   const uint8_t *Hs, int n, const int *ssm,
                                                   uint2 *prof, void *bnd, uint32_t *dir)
 {
     EdgeD *b = (EdgeD *)bnd;
     const int go = kp.go, ge = kp.ge, cap = kp.rows_cap;
-    if (dir16_use(kp, m, n)) {
+    DirOut d;
+    if (CHK || dir16_mode(kp, m, n) == 1) {
         switch (dir16_rows(m, cap)) {
-        case 1: return dp_warp_dir16<TIE, 1, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-        case 2: return dp_warp_dir16<TIE, 2, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-        case 3: return dp_warp_dir16<TIE, 3, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-        case 4: return dp_warp_dir16<TIE, 4, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-        case 5: return dp_warp_dir16<TIE, 5, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-        case 6: return dp_warp_dir16<TIE, 6, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-        case 7: return dp_warp_dir16<TIE, 7, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-        default: return dp_warp_dir16<TIE, 8, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+        case 1: d = dp_warp_dir16<TIE, 1, LOCAL, CHK>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+        case 2: d = dp_warp_dir16<TIE, 2, LOCAL, CHK>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+        case 3: d = dp_warp_dir16<TIE, 3, LOCAL, CHK>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+        case 4: d = dp_warp_dir16<TIE, 4, LOCAL, CHK>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+        case 5: d = dp_warp_dir16<TIE, 5, LOCAL, CHK>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+        case 6: d = dp_warp_dir16<TIE, 6, LOCAL, CHK>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+        case 7: d = dp_warp_dir16<TIE, 7, LOCAL, CHK>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+        default: d = dp_warp_dir16<TIE, 8, LOCAL, CHK>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
         }
+        if (!CHK || !d.sat) return d;
+        // a value left int16's safe range: redo the region on 32-bit lanes (the
+        // profile buffer and arena slot hold either form)
     }
     switch (dir_rows(m, cap)) {
-    case 1: return dp_warp_dir<TIE, 1, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-    case 2: return dp_warp_dir<TIE, 2, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-    case 3: return dp_warp_dir<TIE, 3, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-    case 4: return dp_warp_dir<TIE, 4, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-    case 5: return dp_warp_dir<TIE, 5, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-    case 6: return dp_warp_dir<TIE, 6, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-    case 7: return dp_warp_dir<TIE, 7, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
-    default: return dp_warp_dir<TIE, 8, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir);
+    case 1: d = dp_warp_dir<TIE, 1, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+    case 2: d = dp_warp_dir<TIE, 2, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+    case 3: d = dp_warp_dir<TIE, 3, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+    case 4: d = dp_warp_dir<TIE, 4, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+    case 5: d = dp_warp_dir<TIE, 5, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+    case 6: d = dp_warp_dir<TIE, 6, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+    case 7: d = dp_warp_dir<TIE, 7, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
+    default: d = dp_warp_dir<TIE, 8, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, b, dir); break;
     }
+    d.sat = CHK ? 1 : 0;
+    return d;
 }
 
 // ---------------------------------------------------------------- X-drop
 // DP of each seed region of the tasks [t0, t1); a task's regions sit at
-// arena + doff[t] - doff[t0] (seed 0 first).  dsc[2p + s] = global score.
-template <int TIE>
+// arena + doff[t] - doff[t0] (seed 0 first).  dsc[2p + s] = global score,
+// dsc[2n + 2p + s] = 1 where a checked 16-bit region was redone on 32-bit lanes.
+template <int TIE, bool CHK>
 __global__ void __launch_bounds__(WARPS * 32, 2) k_ga_dir(const KParams kp, uint64_t t0, uint64_t t1,
                                                          const uint64_t *doff, uint8_t *arena, int *dsc)
 {
@@ -148,7 +179,7 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga_dir(const KParams kp, uint
     const uint64_t base = doff[t0];
     WarpQueue q;
     uint64_t u;
-    while (q.pop(&kp.counter[3], t1 - t0, u)) {
+    while (q.pop(&kp.counter[CHK ? 0 : 3], t1 - t0, u)) {
         const uint64_t t = t0 + u;
         const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
         if (p >= kp.n) continue;
@@ -158,15 +189,18 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga_dir(const KParams kp, uint
         if (!pair_seqs(kp, pr, V, m, Hs, n)) continue;
         const SeedPlan sp = seed_plan(kp, p);
         uint64_t off = doff[t] - base;
-#pragma unroll
+        // one copy of the DP dispatch for both seeds (its instantiations are many)
+#pragma unroll 1
         for (int s = 0; s < 2; ++s) {
             if (!sp.dp[s]) continue;
             const XdRec &r = sp.rec[s];
             const int rm = r.ev - r.bv, rn = r.eh - r.bh;
-            const DirOut d = dp_dispatch_dir<TIE, false>(kp, V + r.bv, rm, Hs + r.bh, rn, ssm, prof,
-                                                         bnd, (uint32_t *)(arena + off));
-            if (lane == 0) dsc[2 * p + s] = d.score;
-            exec += (uint64_t)rm * (uint64_t)rn;
+            if ((dir16_mode(kp, rm, rn) == 2) == CHK) {     // this pass's regions only
+                const DirOut d = dp_dispatch_dir<TIE, false, CHK>(kp, V + r.bv, rm, Hs + r.bh, rn, ssm,
+                                                                  prof, bnd, (uint32_t *)(arena + off));
+                if (lane == 0) { dsc[2 * p + s] = d.score; dsc[2 * kp.n + 2 * p + s] = d.sat; }
+                exec += (uint64_t)rm * (uint64_t)rn;
+            }
             off += region_bytes(kp, rm, rn);
         }
     }
@@ -196,7 +230,7 @@ __device__ __forceinline__ void walk_both(const KParams &kp, const uint32_t *con
 // record k_ga writes.  Five resident blocks per SM (48 registers, a few
 // spilled) measured 1 % faster than four: the walks wait on memory, so more
 // of them in flight count for more than the spills.
-__global__ void __launch_bounds__(256, 5) k_tb_ga(const KParams kp, uint64_t t0, uint64_t t1,
+static __global__ void __launch_bounds__(256, 5) k_tb_ga(const KParams kp, uint64_t t0, uint64_t t1,
                                                const uint64_t *doff, const uint8_t *arena,
                                                const int *dsc)
 {
@@ -250,7 +284,7 @@ __global__ void __launch_bounds__(256, 5) k_tb_ga(const KParams kp, uint64_t t0,
             Hs[s] = Hss + rec.bh;
             if (rm[s] > 0 && rn[s] > 0) {
                 act[s] = true;
-                w16[s] = dir16_use(kp, rm[s], rn[s]);
+                w16[s] = region16(kp, rm[s], rn[s], dsc[2 * kp.n + 2 * p + s]);
                 dm[s] = (const uint32_t *)(arena + off);
                 off += region_bytes(kp, rm[s], rn[s]);
             }
@@ -299,8 +333,9 @@ __global__ void __launch_bounds__(256, 5) k_tb_ga(const KParams kp, uint64_t t0,
 }
 
 // ---------------------------------------------------------------- SW
-// local DP of the tasks [t0, t1); dsc[4p ..] = score, end row, end column, have
-template <int TIE>
+// local DP of the tasks [t0, t1); dsc[4p ..] = score, end row, end column,
+// have | 2 if a checked 16-bit region was redone on 32-bit lanes
+template <int TIE, bool CHK>
 __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint64_t t0, uint64_t t1,
                                                       const uint64_t *doff, uint8_t *arena, int *dsc)
 {
@@ -315,7 +350,7 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint
     const uint64_t base = doff[t0];
     WarpQueue q;
     uint64_t u;
-    while (q.pop(&kp.counter[3], t1 - t0, u)) {
+    while (q.pop(&kp.counter[CHK ? 0 : 3], t1 - t0, u)) {
         const uint64_t t = t0 + u;
         const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
         if (p >= kp.n) continue;
@@ -323,15 +358,16 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint
         const uint8_t *V, *Hs;
         int m, n;
         if (!pair_seqs(kp, pr, V, m, Hs, n)) continue;
+        if ((dir16_mode(kp, m, n) == 2) != CHK) continue;   // this pass's pairs only
         exec += (unsigned long long)m * (unsigned long long)n;
         DirOut d;
         d.score = 0; d.ei = 0; d.ej = 0; d.have = 0;
         if (m > 0 && n > 0)
-            d = dp_dispatch_dir<TIE, true>(kp, V, m, Hs, n, ssm, prof, bnd,
-                                           (uint32_t *)(arena + (doff[t] - base)));
+            d = dp_dispatch_dir<TIE, true, CHK>(kp, V, m, Hs, n, ssm, prof, bnd,
+                                                (uint32_t *)(arena + (doff[t] - base)));
         if (lane == 0) {
             int4 *o = reinterpret_cast<int4 *>(dsc) + p;
-            *o = make_int4(d.score, d.ei, d.ej, d.have);
+            *o = make_int4(d.score, d.ei, d.ej, d.have | (d.sat << 1));
         }
     }
     if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
@@ -339,7 +375,7 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint
 
 // traceback and result of the tasks [t0, t1), one thread per task: the same
 // record k_sw writes
-__global__ void __launch_bounds__(256) k_tb_sw(const KParams kp, uint64_t t0, uint64_t t1,
+static __global__ void __launch_bounds__(256) k_tb_sw(const KParams kp, uint64_t t0, uint64_t t1,
                                                const uint64_t *doff, const uint8_t *arena,
                                                const int *dsc)
 {
@@ -362,10 +398,10 @@ __global__ void __launch_bounds__(256) k_tb_sw(const KParams kp, uint64_t t0, ui
         }
         o.cells = sat_u32((uint64_t)m * (uint64_t)n);
         const int4 d = reinterpret_cast<const int4 *>(dsc)[p];
-        if (m > 0 && n > 0 && d.w) {
+        if (m > 0 && n > 0 && (d.w & 1)) {
             const uint32_t *dm = (const uint32_t *)(arena + (doff[t] - base));
             const TraceOut tr =
-                dir16_use(kp, m, n)
+                region16(kp, m, n, d.w >> 1)
                     ? trace_walk<true, true>(dm, n, dir16_rows(m, kp.rows_cap), d.y, d.z, V, Hs, ssm,
                                              kp.go, kp.ge, d.x)
                     : trace_walk<true, false>(dm, n, dir_rows(m, kp.rows_cap), d.y, d.z, V, Hs, ssm,
