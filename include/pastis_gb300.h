@@ -184,8 +184,10 @@ typedef struct pg_tuning {
                                    beyond that) and a traceback pass counts the statistics;
                                    2: the same, with two cells per instruction on 16-bit
                                    lanes for every region whose scores provably fit 16 bits
-                                   ((m + n + 4) * largest |score| <= 30000), 32-bit lanes for
-                                   the rest; no graph capture in either form */
+                                   ((m + n + 4) * largest |score| <= 30000); larger regions
+                                   whose borders fit run there checked and are redone on
+                                   32-bit lanes if a value leaves [-30000, 30000]; 32-bit
+                                   lanes for the rest; no graph capture in either form */
     int32_t dir_arena_mb;       /* cap on that arena in MiB; 0 = a third of the device memory */
     int32_t xd_stepped;         /* X-drop extension, a thread per (pair, seed): 1 steps one
                                    extension direction at a time and starts the next the
