@@ -314,7 +314,7 @@ def run_gpu(args, rank, world, local_rank):
         form = ctx.get_tuning().dp_traceback
         # 16-bit lanes: each packed op advances two cells, so the same op rate
         # bounds twice the cells (the conservative peak for a mixed batch)
-        cells_per_op = 2 if form == 2 else 1
+        cells_per_op = 2 if form >= 2 else 1
         peak_gcups = peak_ops * cells_per_op / DPX_OPS_PER_CELL / 1e9
         # dominant kernel: the alignment DP (k_ga / k_sw), its own cells and time
         achieved = exec_dp / (dp_ms * 1e-3) / 1e9
@@ -322,7 +322,9 @@ def run_gpu(args, rank, world, local_rank):
         dp_kernel = {0: "k_ga" if mode else "k_sw",
                      1: "k_ga_dir + k_tb_ga" if mode else "k_sw_dir + k_tb_sw",
                      2: ("k_ga_dir + k_tb_ga" if mode else "k_sw_dir + k_tb_sw")
-                     + " (16-bit lanes)"}[form]
+                     + " (16-bit lanes)",
+                     3: ("k_ga_dir + k_tb_ga" if mode else "k_sw_dir + k_tb_sw")
+                     + " (16-bit lanes, two regions per warp)"}[form]
         tpath = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tpath):
             # ncu DRAM bytes per pair of the same kernel on this workload

@@ -187,7 +187,9 @@ typedef struct pg_tuning {
                                    ((m + n + 4) * largest |score| <= 30000); larger regions
                                    whose borders fit run there checked and are redone on
                                    32-bit lanes if a value leaves [-30000, 30000]; 32-bit
-                                   lanes for the rest; no graph capture in either form */
+                                   lanes for the rest; 3: form 2, with the 16-bit regions
+                                   of up to 32 * rows_max rows two per warp, each on half
+                                   of it; no graph capture in these forms */
     int32_t dir_arena_mb;       /* cap on that arena in MiB; 0 = a third of the device memory */
     int32_t xd_stepped;         /* X-drop extension, a thread per (pair, seed): 1 steps one
                                    extension direction at a time and starts the next the
@@ -198,7 +200,7 @@ typedef struct pg_tuning {
                                    from DRAM) */
 } pg_tuning;                    /* 36 bytes */
 
-/* The built-in tuning.  A new context starts from it with dp_traceback = 2
+/* The built-in tuning.  A new context starts from it with dp_traceback = 3
  * (measured fastest in both modes); with a score table whose magnitudes pass
  * 100 (no region fits 16 bits) it takes 1 for PG_MODE_SW and keeps 0 for
  * PG_MODE_XDROP. */

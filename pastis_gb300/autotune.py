@@ -27,7 +27,7 @@ GRID = {
     "xd_blocks_per_sm": (4, 0),      # 0 = occupancy limit (7 on GB300)
     "bucket_order": (1, 0),
     "xd_stepped": (1, 0),            # X-drop extension: a direction per step, or run to end
-    "dp_traceback": (2, 0),          # 2 = traceback form on 16-bit lanes, 0 = statistics
+    "dp_traceback": (3, 0),          # 3 = traceback form on 16-bit lanes, 0 = statistics
 }
 
 
@@ -117,7 +117,7 @@ def tune(ctx, run, key=None, device=0, reps=3, grid=None, use_cache=True, log=No
               "candidates": len(rows), "validated_on_full_batch": validated, "default_ms": next(
                   (m for m, c in rows if c == {"dp_blocks_per_sm": 0, "xd_blocks_per_sm": 0,
                                                "bucket_order": 1, "graph": 0,
-                                               "xd_stepped": 1, "dp_traceback": 2}),
+                                               "xd_stepped": 1, "dp_traceback": 3}),
                   None)}
     if entry:
         try:

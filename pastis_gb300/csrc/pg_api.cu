@@ -160,7 +160,7 @@ struct pg_ctx {
     // launch tuning and the captured graph of the last batch shape
     pg_tuning tune{};
     int dp_per_sm = 1, xd_per_sm = 1;   // occupancy limits
-    int lim16 = 0;                      // largest m + n for 16-bit lanes (dp_traceback 2)
+    int lim16 = 0;                      // largest m + n for 16-bit lanes (dp_traceback 2 and 3)
     uint64_t epoch = 0;                 // bumped whenever a buffer a graph holds moves
     cudaGraphExec_t gexec = nullptr;
     struct GraphKey {
@@ -337,7 +337,7 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     // 10.9 ms; xdrop1m: 72.8 / 78.6 / 57.9 ms).  With a score table too wide
     // for 16 bits every region would take 32-bit lanes, where the X-drop
     // global alignment is faster with statistics.
-    c->tune.dp_traceback = c->lim16 > 0 ? 2 : (cfg->mode == PG_MODE_SW ? 1 : 0);
+    c->tune.dp_traceback = c->lim16 > 0 ? 3 : (cfg->mode == PG_MODE_SW ? 1 : 0);
 #undef CUD
     *out = c;
     return PG_OK;
@@ -571,7 +571,8 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
     kp.order = c->tune.bucket_order ? c->d_order : nullptr;
     kp.rows_cap = c->tune.rows_max;
     kp.dir = c->tune.dp_traceback ? 1 : 0;
-    kp.dir16_lim = c->tune.dp_traceback == 2 ? c->lim16 : 0;
+    kp.dir16_lim = c->tune.dp_traceback >= 2 ? c->lim16 : 0;
+    kp.dir16_pair = c->tune.dp_traceback == 3 ? 1 : 0;
     // regions past dir16_lim run the checked 16-bit form while their borders fit:
     // local borders are 0, global ones go + (i - 1) * max(go, ge) >= -30000
     kp.dir16_side = 0;
@@ -773,7 +774,7 @@ int pg_set_tuning(pg_ctx *c, const pg_tuning *t)
     if (t->rows_max < 1 || t->rows_max > 8) return fail(PG_ERR_ARG, "rows_max %d outside 1..8", t->rows_max);
     if (t->graph != 0 && t->graph != 1) return fail(PG_ERR_ARG, "graph must be 0 or 1");
     if (t->xd_int16 != 0 && t->xd_int16 != 1) return fail(PG_ERR_ARG, "xd_int16 must be 0 or 1");
-    if (t->dp_traceback < 0 || t->dp_traceback > 2) return fail(PG_ERR_ARG, "dp_traceback must be 0, 1 or 2");
+    if (t->dp_traceback < 0 || t->dp_traceback > 3) return fail(PG_ERR_ARG, "dp_traceback must be 0..3");
     if (t->dir_arena_mb < 0) return fail(PG_ERR_ARG, "dir_arena_mb must be >= 0");
     if (t->xd_stepped < -1 || t->xd_stepped > 1) return fail(PG_ERR_ARG, "xd_stepped must be -1, 0 or 1");
     c->tune = *t;

@@ -343,4 +343,203 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
     return res;
 }
 
+// ---------------------------------------------------------------- two regions per warp
+// A region of at most 32 R rows whose values provably fit int16 runs on half a
+// warp: lanes 0-15 take one region, lanes 16-31 another of the same R, each
+// half a wavefront of 32 virtual lanes over a single stripe.  A wavefront
+// spends a step per virtual lane filling and another draining; on half a warp
+// those ramps are half as long, and the two regions share every instruction.
+// Layout of a region: the nibbles of virtual lane v (0..31) at wavefront step
+// k = j - 1 + v in word k * 32 + v, a half-warp's two virtual lanes per lane
+// stored as one 8-byte word (128 contiguous bytes per half-warp and step).
+
+// rows per lane of a region on half a warp (m <= 256)
+__host__ __device__ __forceinline__ int dir16_pair_rows(int m) { return m > 32 ? (m + 31) / 32 : 1; }
+
+__host__ __device__ __forceinline__ uint64_t dir16_pair_bytes(int m, int n)
+{
+    if (m <= 0 || n <= 0) return 0;
+    return (uint64_t)(n + 31) * 128ull;
+}
+
+// Each lane passes its half-warp's region (m = 0: none); R >= dir16_pair_rows(m)
+// for both.  The result is that of the lane's own region.
+template <int TIE, int R, bool LOCAL>
+__device__ DirOut dp_pair_dir16(const uint8_t *__restrict__ V, int m,
+                                const uint8_t *__restrict__ Hs, int n,
+                                const int *__restrict__ ssm, uint2 *__restrict__ prof,
+                                int go, int ge, uint32_t *__restrict__ dir)
+{
+    static_assert(R >= 1 && R <= 8, "a direction word holds 8 rows");
+    const int lane = threadIdx.x & 31;
+    const int sl = lane & 15;                     // lane within the half-warp
+    constexpr bool E_FIRST = (TIE & TIE_E_BEFORE_F) != 0;
+    constexpr bool OPEN_FIRST = (TIE & TIE_OPEN_FIRST) != 0;
+    const int gmax = go > ge ? go : ge;
+    const uint32_t go2 = pk16(go, go), ge2 = pk16(ge, ge);
+    uint2 *profLo = prof, *profHi = prof + NC16 * 32;
+    const bool has = m > 0 && n > 0;
+    const int v_last = has ? (m - 1) / R : -1;   // <= 31
+    const int t_last = has ? v_last >> 1 : -1;
+    const bool lane_on = sl <= t_last;
+    const int hi_on = (2 * sl + 1 <= v_last) ? 1 : 0;
+    const int i_base = 2 * sl * R;                // row above the low half
+    __syncwarp();
+    {
+        int vc[2 * R];
+#pragma unroll
+        for (int r = 0; r < 2 * R; ++r) {
+            const int i = i_base + r + 1;
+            vc[r] = (lane_on && i <= m) ? (int)__ldg(V + i - 1) : -1;
+        }
+        for (int q = 0; q < NC16; ++q) {
+            int c = q + lane;
+            if (c >= NC16) c -= NC16;
+            if (c >= NC16) c -= NC16;
+            uint32_t w[4] = {0x80808080u, 0x80808080u, 0x80808080u, 0x80808080u};
+            if (c < NCODES) {
+#pragma unroll
+                for (int r = 0; r < 2 * R; ++r) {
+                    const int h = r / R, rr = r - h * R;
+                    const uint32_t b = vc[r] >= 0 ? ((uint32_t)ssm[vc[r] * 32 + c] & 0xffu) : 0x80u;
+                    const int wi = 2 * h + (rr >> 2), sh = 8 * (rr & 3);
+                    w[wi] = (w[wi] & ~(0xffu << sh)) | (b << sh);
+                }
+            }
+            profLo[c * 32 + lane] = make_uint2(w[0], w[1]);
+            profHi[c * 32 + lane] = make_uint2(w[2], w[3]);
+        }
+    }
+    __syncwarp();
+    uint32_t Hl[R], Al[R], Gl[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int h0 = dir_col0<LOCAL>(min(i_base + r + 1, m), go, ge, gmax).h;
+        Hl[r] = pk16(h0, NEG16);
+        Al[r] = pk16(NEG16 + ge, NEG16);
+        Gl[r] = pk16(h0 + go, NEG16 + go);
+    }
+    const EdgeD e_up = dir_col0<LOCAL>(min(i_base, m), go, ge, gmax);
+    const EdgeD e_lo = dir_col0<LOCAL>(min(i_base + R, m), go, ge, gmax);
+    const EdgeD e_hi = dir_col0<LOCAL>(min(i_base + 2 * R, m), go, ge, gmax);
+    uint32_t in_h = pk16(e_up.h, e_lo.h), in_a = pk16(c16(e_up.a), c16(e_lo.a));
+    uint32_t out_h = pk16(e_lo.h, e_hi.h), out_a = pk16(c16(e_lo.a), c16(e_hi.a));
+    const uint32_t in_sel = sl == 0 ? 0x5410u : 0x5432u;
+    int hc_lo = SENT16;
+    int hc_next = SENT16;
+    {
+        const int j1 = -2 * sl + 1;
+        if (j1 >= 1 && j1 <= n) hc_next = (int)__ldg(Hs + j1 - 1);
+    }
+    uint2 *dstep = reinterpret_cast<uint2 *>(dir) + sl;
+    uint32_t sbs = 0, sbs_seen = 0;
+    int sbp0 = 0, sbp1 = 0;
+    int nsteps = has ? n + v_last : 0;
+    nsteps = max(nsteps, __shfl_xor_sync(FULL, nsteps, 16));
+    for (int k = 0; k < nsteps; ++k) {
+        const uint32_t rh = __shfl_up_sync(FULL, out_h, 1, 16);
+        const uint32_t ra = __shfl_up_sync(FULL, out_a, 1, 16);
+        const uint32_t dgH = in_h;
+        const int j = k - 2 * sl + 1;
+        // row 0 for the first lane of each half-warp, selected without a branch
+        const int b0 = LOCAL ? 0 : c16(go + (j - 1) * gmax);
+        const uint32_t th = sl == 0 ? (uint32_t)b0 : rh;
+        const uint32_t ta = sl == 0 ? (uint32_t)NEG16 : ra;
+        in_h = prmt(th, out_h, in_sel);
+        in_a = prmt(ta, out_a, in_sel);
+        const int hc_hi = hc_lo;
+        hc_lo = hc_next;
+        {
+            const int jn = j + 1;
+            hc_next = (jn >= 1 && jn <= n) ? (int)__ldg(Hs + jn - 1) : SENT16;
+        }
+        if (lane_on && j >= 1 && j <= n + hi_on) {
+            const uint2 pl = profLo[hc_lo * 32 + lane];
+            const uint2 ph = profHi[hc_hi * 32 + lane];
+            uint32_t cA = in_a, cG = v16add(in_h, go2);
+            uint32_t dH = dgH;
+            uint32_t W0 = 0, W1 = 0;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const uint32_t s2 = prmt(r < 4 ? pl.x : pl.y, r < 4 ? ph.x : ph.y, sx_sel(r & 3));
+                const uint32_t E = v16max(Al[r], Gl[r]);
+                const uint32_t pe = OPEN_FIRST ? (v16ne(E, Gl[r]) ^ ONE2) : v16ne(E, Al[r]);
+                const uint32_t dg = v16add(dH, s2);
+                const uint32_t X = v16max(dg, E);
+                const uint32_t F = v16max(cA, cG);
+                const uint32_t pf = OPEN_FIRST ? (v16ne(F, cG) ^ ONE2) : v16ne(F, cA);
+                const uint32_t Hv = LOCAL ? __vimax_s16x2_relu(X, F) : v16max(X, F);
+                const uint32_t nd = v16ne(Hv, dg);
+                const uint32_t ne = E_FIRST ? (v16ne(Hv, E) ^ ONE2) : v16ne(Hv, F);
+                const uint32_t nib = nd + 2u * ne + 4u * pe + 8u * pf;
+                if (r < 4) W0 += nib << (4 * (r & 3));
+                else W1 += nib << (4 * (r & 3));
+                const uint32_t G = v16add(Hv, go2);
+                cA = v16add(F, ge2);
+                cG = G;
+                dH = Hl[r];
+                Hl[r] = Hv;
+                Al[r] = v16add(E, ge2);
+                Gl[r] = G;
+                if (LOCAL) sbs = v16max(sbs, Hv);
+            }
+            dstep[(uint64_t)k * 16u] = make_uint2(prmt(W0, W1, 0x5410u), prmt(W0, W1, 0x7632u));
+            out_h = Hl[R - 1];
+            out_a = cA;
+            if (LOCAL && sbs != sbs_seen) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int s = half16(sbs, h);
+                    if (s != half16(sbs_seen, h)) {
+                        int rr = R - 1;
+#pragma unroll
+                        for (int r = R - 1; r >= 0; --r)
+                            if (half16(Hl[r], h) == s) rr = r;
+                        const int p = ((j - h) << 3) | rr;
+                        if (h) sbp1 = p; else sbp0 = p;
+                    }
+                }
+                sbs_seen = sbs;
+            }
+        }
+    }
+    __syncwarp();
+    DirOut res;
+    res.have = 0; res.ei = 0; res.ej = 0; res.score = 0;
+    if (LOCAL) {
+        // first maximum in column-major order: the low half's rows before the
+        // high half's in a column, then the smaller column, then the smaller row
+        int bs = 0, bi = 0, bj = 0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int s = half16(sbs, h);
+            const int sp = h ? sbp1 : sbp0;
+            const int sj = sp >> 3;
+            if (s > 0 && (s > bs || (s == bs && sj < bj))) {
+                bs = s; bj = sj; bi = i_base + h * R + (sp & 7) + 1;
+            }
+        }
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+            const int os = __shfl_xor_sync(FULL, bs, o);
+            const int oi = __shfl_xor_sync(FULL, bi, o);
+            const int oj = __shfl_xor_sync(FULL, bj, o);
+            const bool take = os > bs || (os == bs && (oj < bj || (oj == bj && oi < bi)));
+            if (take) { bs = os; bi = oi; bj = oj; }
+        }
+        res.score = bs;
+        res.have = bs > 0;
+        res.ei = bi; res.ej = bj;
+    } else {
+        const int rl = has ? (m - 1) % R : -1;
+        const int h = v_last & 1;
+        int hs = 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            if (r == rl) hs = half16(Hl[r], h);
+        res.score = __shfl_sync(FULL, hs, (lane & 16) + (t_last > 0 ? t_last : 0));
+    }
+    return res;
+}
+
 }  // namespace pg

@@ -83,6 +83,7 @@ struct KParams {
     int dir = 0;                     // 1: the traceback form (pg_kernels_dir.cuh) runs the DP
     int dir16_lim = 0;               // traceback form: regions with m + n <= this on 16-bit lanes
     int dir16_side = 0;              // ... and larger ones with both sides <= this, checked
+    int dir16_pair = 0;              // 1: 16-bit regions of up to 32 x rows_cap rows two per warp
 };
 
 __device__ __forceinline__ void load_sm(int *ssm, const int8_t *sm)
@@ -236,10 +237,24 @@ __host__ __device__ __forceinline__ bool dir16_use(const KParams &kp, int m, int
     return dir16_mode(kp, m, n) != 0;
 }
 
-// traceback form: rows per lane of the region's DP, 16-bit lanes (12..19) after 32-bit (4..11)
+// a region whose DP runs on half a warp, two regions per warp (dp_pair_dir16):
+// every value provably inside int16 and one stripe of 32 x rows_cap rows
+__host__ __device__ __forceinline__ bool dir16_paired(const KParams &kp, int m, int n)
+{
+    const int cap = kp.rows_cap < 8 ? kp.rows_cap : 8;
+    return kp.dir16_pair && dir16_mode(kp, m, n) == 1 && m <= 32 * cap;
+}
+
+// traceback form: rows per lane of the region's DP, 16-bit lanes (12..19) after
+// 32-bit (4..11); with two regions per warp, the half-warp regions by their
+// rows per lane (12..19) and the rest of the 16-bit ones first (0..3)
 __device__ __forceinline__ int dir_bucket(const KParams &kp, int m, int n)
 {
-    if (dir16_use(kp, m, n)) return 20 - dir16_rows(m, kp.rows_cap);
+    if (dir16_use(kp, m, n)) {
+        if (!kp.dir16_pair) return 20 - dir16_rows(m, kp.rows_cap);
+        if (dir16_paired(kp, m, n)) return 20 - dir16_pair_rows(m);
+        return max(0, 8 - dir16_rows(m, kp.rows_cap));
+    }
     return 12 - dp_rows_per_lane<S1>(m, kp.rows_cap);
 }
 

@@ -43,6 +43,7 @@ __device__ __forceinline__ SeedPlan seed_plan(const KParams &kp, uint64_t p)
 // otherwise, room for either where a checked region may be redone
 __device__ __forceinline__ uint64_t region_bytes(const KParams &kp, int m, int n)
 {
+    if (dir16_paired(kp, m, n)) return dir16_pair_bytes(m, n);
     const int mode = dir16_mode(kp, m, n);
     const uint64_t b16 = mode ? dir16_bytes(m, n, dir16_rows(m, kp.rows_cap)) : 0;
     const uint64_t b32 = mode != 1 ? dir_bytes(m, n, dir_rows(m, kp.rows_cap)) : 0;
@@ -55,6 +56,14 @@ __device__ __forceinline__ bool region16(const KParams &kp, int m, int n, int re
 {
     const int mode = dir16_mode(kp, m, n);
     return mode == 1 || (mode == 2 && !redone);
+}
+
+// rows per lane and lanes of the wavefront of a region's direction words
+__device__ __forceinline__ void region_layout(const KParams &kp, int m, int n, bool w16, int &R, int &vl)
+{
+    if (!w16) { R = dir_rows(m, kp.rows_cap); vl = 32; }
+    else if (dir16_paired(kp, m, n)) { R = dir16_pair_rows(m); vl = 32; }
+    else { R = dir16_rows(m, kp.rows_cap); vl = 64; }
 }
 
 // this warp's score profile in the dynamic shared memory of the traceback DP
@@ -160,6 +169,80 @@ __device__ __forceinline__ DirOut dp_dispatch_dir(const KParams &kp, const uint8
     return d;
 }
 
+// the DP of two regions of R rows per lane on the two halves of the warp (each
+// lane passes its own half's region; m = 0: none)
+template <int TIE, bool LOCAL>
+__device__ __forceinline__ DirOut dp_dispatch_pair(const KParams &kp, int R, const uint8_t *V, int m,
+                                                   const uint8_t *Hs, int n, const int *ssm,
+                                                   uint2 *prof, uint32_t *dir)
+{
+    const int go = kp.go, ge = kp.ge;
+    switch (R) {
+    case 1: return dp_pair_dir16<TIE, 1, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, dir);
+    case 2: return dp_pair_dir16<TIE, 2, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, dir);
+    case 3: return dp_pair_dir16<TIE, 3, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, dir);
+    case 4: return dp_pair_dir16<TIE, 4, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, dir);
+    case 5: return dp_pair_dir16<TIE, 5, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, dir);
+    case 6: return dp_pair_dir16<TIE, 6, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, dir);
+    case 7: return dp_pair_dir16<TIE, 7, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, dir);
+    default: return dp_pair_dir16<TIE, 8, LOCAL>(V, m, Hs, n, ssm, prof, go, ge, dir);
+    }
+}
+
+// A region waiting for a partner of the same rows per lane: lane R of the warp
+// holds key + 1 of the waiting region of R rows per lane (0: none).  X-drop key:
+// task << 1 | seed; SW key: task.
+struct PairSlots {
+    uint64_t pend = 0;
+    // the waiting key + 1 for R (0: none); the slot is then empty, or holds key + 1
+    __device__ __forceinline__ uint64_t swap(int R, uint64_t key1)
+    {
+        const int lane = threadIdx.x & 31;
+        const uint64_t w = __shfl_sync(FULL, pend, R);
+        if (lane == R) pend = w ? 0 : key1;
+        return w;
+    }
+};
+
+// seed s's region of the X-drop task at bucket position t: sequences, sides
+// and arena offset (from the chunk's base); false when the pair has no such DP
+__device__ __forceinline__ bool ga_region(const KParams &kp, uint64_t t, int s, const uint64_t *doff,
+                                          uint64_t base, uint64_t &p, const uint8_t *&V, int &m,
+                                          const uint8_t *&Hs, int &n, uint64_t &off)
+{
+    p = kp.order ? (uint64_t)kp.order[t] : t;
+    if (p >= kp.n) return false;
+    const pg_pair pr = kp.pairs[p];
+    int pm, pn;
+    if (!pair_seqs(kp, pr, V, pm, Hs, pn)) return false;
+    const SeedPlan sp = seed_plan(kp, p);
+    if (!sp.dp[s]) return false;
+    off = doff[t] - base;
+    if (s == 1 && sp.dp[0])
+        off += region_bytes(kp, sp.rec[0].ev - sp.rec[0].bv, sp.rec[0].eh - sp.rec[0].bh);
+    const XdRec r = s ? sp.rec[1] : sp.rec[0];
+    V += r.bv; Hs += r.bh;
+    m = r.ev - r.bv; n = r.eh - r.bh;
+    return true;
+}
+
+// the DP of two waiting X-drop regions (keys a and b, + 1; b = 0: none)
+template <int TIE>
+__device__ __forceinline__ void ga_pair(const KParams &kp, int R, uint64_t a1, uint64_t b1, uint64_t t0,
+                                        const uint64_t *doff, uint64_t base, uint8_t *arena,
+                                        const int *ssm, uint2 *prof, int *dsc)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t k1 = lane < 16 ? a1 : b1;
+    uint64_t p = 0, off = 0;
+    const uint8_t *V = nullptr, *Hs = nullptr;
+    int m = 0, n = 0;
+    const int s = k1 ? (int)((k1 - 1) & 1) : 0;
+    if (!k1 || !ga_region(kp, t0 + ((k1 - 1) >> 1), s, doff, base, p, V, m, Hs, n, off)) m = n = 0;
+    const DirOut d = dp_dispatch_pair<TIE, false>(kp, R, V, m, Hs, n, ssm, prof, (uint32_t *)(arena + off));
+    if ((lane & 15) == 0 && m > 0) { dsc[2 * p + s] = d.score; dsc[2 * kp.n + 2 * p + s] = 0; }
+}
+
 // ---------------------------------------------------------------- X-drop
 // DP of each seed region of the tasks [t0, t1); a task's regions sit at
 // arena + doff[t] - doff[t0] (seed 0 first).  dsc[2p + s] = global score,
@@ -195,7 +278,8 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga_dir(const KParams kp, uint
             if (!sp.dp[s]) continue;
             const XdRec &r = sp.rec[s];
             const int rm = r.ev - r.bv, rn = r.eh - r.bh;
-            if ((dir16_mode(kp, rm, rn) == 2) == CHK) {     // this pass's regions only
+            // this pass's regions only (the half-warp ones run in k_ga_pair)
+            if ((dir16_mode(kp, rm, rn) == 2) == CHK && (CHK || !dir16_paired(kp, rm, rn))) {
                 const DirOut d = dp_dispatch_dir<TIE, false, CHK>(kp, V + r.bv, rm, Hs + r.bh, rn, ssm,
                                                                   prof, bnd, (uint32_t *)(arena + off));
                 if (lane == 0) { dsc[2 * p + s] = d.score; dsc[2 * kp.n + 2 * p + s] = d.sat; }
@@ -203,6 +287,61 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga_dir(const KParams kp, uint
             }
             off += region_bytes(kp, rm, rn);
         }
+    }
+    if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
+}
+
+// DP of the half-warp regions (dir16_paired) of the tasks [t0, t1), two per
+// warp: a region waits for a partner of the same rows per lane, and those left
+// without one when the queue runs dry run alone.  Its own kernel: next to the
+// whole-warp DP in one kernel, the whole-warp loop measured 26 % slower.
+template <int TIE>
+__global__ void __launch_bounds__(WARPS * 32, 2) k_ga_pair(const KParams kp, uint64_t t0, uint64_t t1,
+                                                          const uint64_t *doff, uint8_t *arena, int *dsc)
+{
+    __shared__ int ssm[32 * 32];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
+    uint2 *prof = dir_prof(kp);
+    const int lane = threadIdx.x & 31;
+    unsigned long long exec = 0;
+    const uint64_t base = doff[t0];
+    WarpQueue q;
+    PairSlots slots;
+    // one call site of the DP (its instantiations are many): each turn finds
+    // the next two regions, seed by seed, then (flush = R, 1..8) the ones left
+    uint64_t u = 0;
+    int s = 2, flush = 0;           // next seed of the task (2: take a task)
+    SeedPlan sp;
+    for (;;) {
+        uint64_t a1 = 0, b1 = 0;
+        int R = 0;
+        if (flush == 0) {
+            if (s == 2) {
+                if (!q.pop(&kp.counter[0], t1 - t0, u)) { flush = 1; continue; }
+                const uint64_t t = t0 + u;
+                const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
+                if (p >= kp.n) continue;
+                sp = seed_plan(kp, p);
+                s = 0;
+            }
+            const int js = s++;
+            if (!sp.dp[js]) continue;
+            const XdRec r = js ? sp.rec[1] : sp.rec[0];
+            const int rm = r.ev - r.bv, rn = r.eh - r.bh;
+            if (!dir16_paired(kp, rm, rn)) continue;
+            exec += (uint64_t)rm * (uint64_t)rn;
+            R = dir16_pair_rows(rm);
+            b1 = ((u << 1) | (uint64_t)js) + 1;
+            a1 = slots.swap(R, b1);
+            if (!a1) continue;
+        } else {
+            if (flush > 8) break;
+            R = flush++;
+            a1 = __shfl_sync(FULL, slots.pend, R);
+            if (!a1) continue;
+        }
+        ga_pair<TIE>(kp, R, a1, b1, t0, doff, base, arena, ssm, prof, dsc);
     }
     if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
 }
@@ -215,10 +354,11 @@ __device__ __forceinline__ void walk_both(const KParams &kp, const uint32_t *con
                                           const uint8_t *const Hs[2], const int *ssm,
                                           const bool act[2], TraceOut tr[2])
 {
-    Walker<false, WA> a(dm[0], rn[0], WA ? dir16_rows(rm[0], kp.rows_cap) : dir_rows(rm[0], kp.rows_cap),
-                        rm[0], rn[0], V[0], Hs[0], ssm, kp.go, kp.ge, 0);
-    Walker<false, WB> b(dm[1], rn[1], WB ? dir16_rows(rm[1], kp.rows_cap) : dir_rows(rm[1], kp.rows_cap),
-                        rm[1], rn[1], V[1], Hs[1], ssm, kp.go, kp.ge, 0);
+    int Ra, vla, Rb, vlb;
+    region_layout(kp, rm[0], rn[0], WA, Ra, vla);
+    region_layout(kp, rm[1], rn[1], WB, Rb, vlb);
+    Walker<false, WA> a(dm[0], rn[0], Ra, vla, rm[0], rn[0], V[0], Hs[0], ssm, kp.go, kp.ge, 0);
+    Walker<false, WB> b(dm[1], rn[1], Rb, vlb, rm[1], rn[1], V[1], Hs[1], ssm, kp.go, kp.ge, 0);
     a.done = !act[0];
     b.done = !act[1];
     while (a.step() | b.step()) {}
@@ -333,6 +473,31 @@ static __global__ void __launch_bounds__(256, 5) k_tb_ga(const KParams kp, uint6
 }
 
 // ---------------------------------------------------------------- SW
+// the DP of two waiting SW pairs (task keys a and b, + 1; b = 0: none)
+template <int TIE>
+__device__ __forceinline__ void sw_pair(const KParams &kp, int R, uint64_t a1, uint64_t b1, uint64_t t0,
+                                        const uint64_t *doff, uint64_t base, uint8_t *arena,
+                                        const int *ssm, uint2 *prof, int *dsc)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t k1 = lane < 16 ? a1 : b1;
+    uint64_t p = 0, off = 0;
+    const uint8_t *V = nullptr, *Hs = nullptr;
+    int m = 0, n = 0;
+    if (k1) {
+        const uint64_t t = t0 + (k1 - 1);
+        p = kp.order ? (uint64_t)kp.order[t] : t;
+        const pg_pair pr = kp.pairs[p];
+        if (!pair_seqs(kp, pr, V, m, Hs, n)) m = n = 0;
+        off = doff[t] - base;
+    }
+    const DirOut d = dp_dispatch_pair<TIE, true>(kp, R, V, m, Hs, n, ssm, prof, (uint32_t *)(arena + off));
+    if ((lane & 15) == 0 && m > 0) {
+        int4 *o = reinterpret_cast<int4 *>(dsc) + p;
+        *o = make_int4(d.score, d.ei, d.ej, d.have);
+    }
+}
+
 // local DP of the tasks [t0, t1); dsc[4p ..] = score, end row, end column,
 // have | 2 if a checked 16-bit region was redone on 32-bit lanes
 template <int TIE, bool CHK>
@@ -359,6 +524,7 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint
         int m, n;
         if (!pair_seqs(kp, pr, V, m, Hs, n)) continue;
         if ((dir16_mode(kp, m, n) == 2) != CHK) continue;   // this pass's pairs only
+        if (!CHK && dir16_paired(kp, m, n)) continue;        // k_sw_pair's
         exec += (unsigned long long)m * (unsigned long long)n;
         DirOut d;
         d.score = 0; d.ei = 0; d.ej = 0; d.have = 0;
@@ -369,6 +535,53 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint
             int4 *o = reinterpret_cast<int4 *>(dsc) + p;
             *o = make_int4(d.score, d.ei, d.ej, d.have | (d.sat << 1));
         }
+    }
+    if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
+}
+
+// local DP of the half-warp pairs (dir16_paired) of the tasks [t0, t1), two
+// per warp, as k_ga_pair
+template <int TIE>
+__global__ void __launch_bounds__(WARPS * 32, 2) k_sw_pair(const KParams kp, uint64_t t0, uint64_t t1,
+                                                          const uint64_t *doff, uint8_t *arena, int *dsc)
+{
+    __shared__ int ssm[32 * 32];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
+    uint2 *prof = dir_prof(kp);
+    const int lane = threadIdx.x & 31;
+    unsigned long long exec = 0;
+    const uint64_t base = doff[t0];
+    WarpQueue q;
+    PairSlots slots;
+    // one call site of the DP, as in k_ga_pair
+    int flush = 0;
+    for (;;) {
+        uint64_t a1 = 0, b1 = 0;
+        int R = 0;
+        if (flush == 0) {
+            uint64_t u;
+            if (!q.pop(&kp.counter[0], t1 - t0, u)) { flush = 1; continue; }
+            const uint64_t t = t0 + u;
+            const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
+            if (p >= kp.n) continue;
+            const pg_pair pr = kp.pairs[p];
+            const uint8_t *V, *Hs;
+            int m, n;
+            if (!pair_seqs(kp, pr, V, m, Hs, n)) continue;
+            if (!dir16_paired(kp, m, n)) continue;
+            exec += (unsigned long long)m * (unsigned long long)n;
+            R = dir16_pair_rows(m);
+            b1 = u + 1;
+            a1 = slots.swap(R, b1);
+            if (!a1) continue;
+        } else {
+            if (flush > 8) break;
+            R = flush++;
+            a1 = __shfl_sync(FULL, slots.pend, R);
+            if (!a1) continue;
+        }
+        sw_pair<TIE>(kp, R, a1, b1, t0, doff, base, arena, ssm, prof, dsc);
     }
     if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
 }
@@ -400,12 +613,11 @@ static __global__ void __launch_bounds__(256) k_tb_sw(const KParams kp, uint64_t
         const int4 d = reinterpret_cast<const int4 *>(dsc)[p];
         if (m > 0 && n > 0 && (d.w & 1)) {
             const uint32_t *dm = (const uint32_t *)(arena + (doff[t] - base));
-            const TraceOut tr =
-                region16(kp, m, n, d.w >> 1)
-                    ? trace_walk<true, true>(dm, n, dir16_rows(m, kp.rows_cap), d.y, d.z, V, Hs, ssm,
-                                             kp.go, kp.ge, d.x)
-                    : trace_walk<true, false>(dm, n, dir_rows(m, kp.rows_cap), d.y, d.z, V, Hs, ssm,
-                                              kp.go, kp.ge, d.x);
+            const bool w16 = region16(kp, m, n, d.w >> 1);
+            int R, vl;
+            region_layout(kp, m, n, w16, R, vl);
+            const TraceOut tr = w16 ? trace_walk<true, true>(dm, n, R, vl, d.y, d.z, V, Hs, ssm, kp.go, kp.ge, d.x)
+                                    : trace_walk<true, false>(dm, n, R, vl, d.y, d.z, V, Hs, ssm, kp.go, kp.ge, d.x);
             const uint32_t L = (uint32_t)((d.y - tr.i0) + (d.z - tr.j0)) - tr.D;
             o.score = d.x;
             o.aln_len = L; o.matches = tr.M; o.gap_opens = tr.G;

@@ -1,6 +1,6 @@
 // pg_trace.cuh -- traceback over the direction nibbles of dp_warp_dir
-// (pg_dpdir.cuh, 32 lanes) or dp_warp_dir16 (pg_dpdir16.cuh, 64 virtual
-// lanes): a walk from the region's end cell back to its start that counts
+// (pg_dpdir.cuh, 32 lanes) or dp_warp_dir16 / dp_pair_dir16 (pg_dpdir16.cuh,
+// 64 or 32 virtual lanes): a walk from the region's end cell back to its start that counts
 // what computeAlignmentStats counts (src/align/SeqanFullAligner.cpp:238-246):
 // diagonal columns, identical columns, and gap runs (maximal runs of
 // same-orientation gap moves).
@@ -32,21 +32,21 @@ struct TraceOut {
     int i0, j0;
 };
 
-// A walker over one region.  W16: the nibbles of dp_warp_dir16 (bit 0: not
-// the diagonal, bit 1: E rather than F; a local walk carries the score of the
-// cell it stands on, h, and stops where it is 0).  Otherwise the nibbles of
-// dp_warp_dir (bits 0-1: diagonal, F, E or the local floor).  Words: (s * (n
-// + VL - 1) + k) * VL + v for stripe s, wavefront step k = j - 1 + v, lane v
-// (VL = 32 lanes, or 64 virtual lanes).  ssm: the 32 x 32 substitution table
-// in shared memory (read only by a local W16 walk).  step() makes one move
-// and returns false once the walk has ended; the counts are then final.
+// A walker over one region.  W16: the nibbles of dp_warp_dir16 or
+// dp_pair_dir16 (bit 0: not the diagonal, bit 1: E rather than F; a local walk
+// carries the score of the cell it stands on, h, and stops where it is 0).
+// Otherwise the nibbles of dp_warp_dir (bits 0-1: diagonal, F, E or the local
+// floor).  Words: (s * (n + vl - 1) + k) * vl + v for stripe s, wavefront step
+// k = j - 1 + v, lane v (vl = 32 lanes, 64 virtual lanes of a warp, or 32 of a
+// half-warp).  ssm: the 32 x 32 substitution table in shared memory (read only
+// by a local W16 walk).  step() makes one move and returns false once the walk
+// has ended; the counts are then final.
 template <bool LOCAL, bool W16>
 struct Walker {
-    static constexpr int VL = W16 ? 64 : 32;
     const uint32_t *dir;
     const uint8_t *V, *Hs;
     const int *ssm;
-    int n, R, go, ge;
+    int n, R, vl, go, ge;
     int i, j, h;
     int s = 0, v = 0, r = 0;   // row i - 1 as stripe, lane, row of the lane (kept in step with i)
     int state = 0;             // 0: H, 1: F (vertical gap), 2: E (horizontal gap)
@@ -54,13 +54,14 @@ struct Walker {
     uint32_t M = 0, D = 0, G = 0;
     bool done = false;
 
-    __device__ __forceinline__ Walker(const uint32_t *dir_, int n_, int R_, int i_, int j_,
+    __device__ __forceinline__ Walker(const uint32_t *dir_, int n_, int R_, int vl_, int i_, int j_,
                                       const uint8_t *V_, const uint8_t *Hs_, const int *ssm_,
                                       int go_, int ge_, int h_)
-        : dir(dir_), V(V_), Hs(Hs_), ssm(ssm_), n(n_), R(R_), go(go_), ge(ge_), i(i_), j(j_), h(h_)
+        : dir(dir_), V(V_), Hs(Hs_), ssm(ssm_), n(n_), R(R_), vl(vl_), go(go_), ge(ge_), i(i_), j(j_),
+          h(h_)
     {
         if (i > 0) {
-            const int r0 = i - 1, rows = VL * R;
+            const int r0 = i - 1, rows = vl * R;
             s = r0 / rows;
             const int within = r0 - s * rows;
             v = within / R;
@@ -71,7 +72,7 @@ struct Walker {
     {
         if (--r < 0) {
             r = R - 1;
-            if (--v < 0) { v = VL - 1; --s; }
+            if (--v < 0) { v = vl - 1; --s; }
         }
     }
     __device__ __forceinline__ bool step()
@@ -87,7 +88,7 @@ struct Walker {
         }
         // the word of (i, j) first (i, j >= 1 here): its load does not wait on h,
         // whose substitution-score lookups it overlaps
-        const uint32_t w = __ldg(dir + ((uint64_t)s * (uint64_t)(n + VL - 1) + (uint64_t)(j - 1 + v)) * VL + v);
+        const uint32_t w = __ldg(dir + ((uint64_t)s * (uint64_t)(n + vl - 1) + (uint64_t)(j - 1 + v)) * (uint64_t)vl + v);
         if (W16 && LOCAL && state == 0 && h == 0) { done = true; return false; }
         const uint32_t nib = (w >> (4 * r)) & 15u;
         if (state == 0) {
@@ -136,11 +137,11 @@ struct Walker {
 };
 
 template <bool LOCAL, bool W16>
-__device__ __forceinline__ TraceOut trace_walk(const uint32_t *dir, int n, int R, int i, int j,
+__device__ __forceinline__ TraceOut trace_walk(const uint32_t *dir, int n, int R, int vl, int i, int j,
                                                const uint8_t *V, const uint8_t *Hs, const int *ssm,
                                                int go, int ge, int h)
 {
-    Walker<LOCAL, W16> w(dir, n, R, i, j, V, Hs, ssm, go, ge, h);
+    Walker<LOCAL, W16> w(dir, n, R, vl, i, j, V, Hs, ssm, go, ge, h);
     while (w.step()) {}
     return w.out();
 }

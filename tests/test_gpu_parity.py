@@ -44,9 +44,10 @@ def run_both(mode, w, cfg, O, pairs=None, roff=0, coff=0, share=True):
         ctx.set_seqs(1, ascii_, w.offs)
     got = ctx.align(pairs, roff, coff)
     # traceback form by default: X-drop: k_xdf, k_xd_wide, k_hist, k_bucket,
-    # k_dirsize, k_ga_dir, k_tb_ga; SW: k_hist, k_bucket, k_dirsize, k_sw_dir,
-    # k_tb_sw; one more (the checked 16-bit pass) where long regions need it
-    base = 7 if mode == capi.MODE_XDROP else 5
+    # k_dirsize, k_ga_dir, k_ga_pair, k_tb_ga; SW: k_hist, k_bucket, k_dirsize,
+    # k_sw_dir, k_sw_pair, k_tb_sw; one more (the checked 16-bit pass) where
+    # long regions need it
+    base = 8 if mode == capi.MODE_XDROP else 6
     assert ctx.last_launches() in (base, base + 1)
     codes = O.encode(bytes(ascii_))
     exp = O.batch(mode, codes, w.offs, codes, w.offs, pairs, oracle_params(O, cfg),
@@ -261,7 +262,9 @@ def test_tuning_and_graph_replay_keep_results(native, oracle_mod, mode):
               {"dp_traceback": 1, "dir_arena_mb": 1}, {"dp_traceback": 1, "rows_max": 3},
               {"dp_traceback": 1, "bucket_order": 0, "graph": 1}, {"dp_traceback": 2},
               {"dp_traceback": 2, "dir_arena_mb": 1}, {"dp_traceback": 2, "rows_max": 3},
-              {"dp_traceback": 2, "bucket_order": 0}, {"xd_stepped": 0}, {"xd_stepped": 1},
+              {"dp_traceback": 2, "bucket_order": 0}, {"dp_traceback": 3},
+              {"dp_traceback": 3, "dir_arena_mb": 1}, {"dp_traceback": 3, "rows_max": 3},
+              {"dp_traceback": 3, "bucket_order": 0}, {"xd_stepped": 0}, {"xd_stepped": 1},
               {"xd_stepped": 0, "xd_blocks_per_sm": 2}):
         ctx.set_tuning(capi.default_tuning(), **t)
         for rep in range(2):                 # the second call replays the graph
@@ -325,11 +328,12 @@ def test_int16_extension_saturation_reruns_in_32_bits(native, oracle_mod):
 @pytest.mark.parametrize("tie", [0, 1, 2, 3])
 @pytest.mark.parametrize("gaps", [0, 1])
 @pytest.mark.parametrize("mode", [0, 1])
-@pytest.mark.parametrize("form", [1, 2])
+@pytest.mark.parametrize("form", [1, 2, 3])
 def test_traceback_form_parity(sw_small, xd_small, oracle_mod, tie, gaps, mode, form):
     """The traceback form of the DP (direction nibbles in HBM, then a walk
-    back), on 32-bit lanes (form 1) and 16-bit lanes (form 2), gives the
-    oracle's results under every tie policy and gap model."""
+    back), on 32-bit lanes (form 1), 16-bit lanes (form 2) and 16-bit lanes
+    with two regions per warp (form 3), gives the oracle's results under every
+    tie policy and gap model."""
     from pastis_gb300 import capi
     w = sw_small if mode == capi.MODE_SW else xd_small
     cfg = capi.config(mode, tie=tie, gap_semantics=gaps)
@@ -357,7 +361,7 @@ def test_traceback_form_long_regions(native, oracle_mod):
     for mode in (capi.MODE_SW, capi.MODE_XDROP):
         cfg = capi.config(mode)
         exp = O.batch(mode, codes, w.offs, codes, w.offs, w.pairs, oracle_params(O, cfg))
-        for form in (1, 2):
+        for form in (1, 2, 3):
             ctx = capi.Context(cfg)
             ctx.set_seqs(0, w.ascii, w.offs)
             ctx.share_row_seqs()
@@ -365,6 +369,50 @@ def test_traceback_form_long_regions(native, oracle_mod):
             got = ctx.align(w.pairs)
             assert_same(got, exp, w.pairs)
             ctx.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_pair_form_row_boundaries(native, oracle_mod, mode):
+    """Form 3 runs the 16-bit regions of up to 32 R rows two per warp, each on
+    half of it.  Row counts at and around every multiple of 32 up to 256 (and
+    past it, on the whole warp), partners of very different column counts,
+    enough regions per warp that most find a partner, and a batch of one region
+    of each row count (each runs alone); two tie policies."""
+    from pastis_gb300 import capi
+    O = oracle_mod
+    rng = np.random.default_rng(29)
+    alpha = np.frombuffer(b"ACDEFGHIKLMNPQRSTVWY", dtype=np.uint8)
+    ms = [1, 2, 31, 32, 33, 63, 64, 65, 95, 96, 97, 128, 129, 160, 192, 224, 255, 256, 257, 300]
+    ns = [1, 3, 40, 250, 700]
+    root = rng.integers(0, 20, 800)
+    seqs = []
+    for L in ms + ns:
+        s = root[:L].copy()
+        mut = rng.random(L) < 0.25
+        s[mut] = rng.integers(0, 20, int(mut.sum()))
+        seqs.append(alpha[s].tobytes().decode())
+    w = _toy(seqs)
+    npairs = 12000
+    pairs = np.zeros(npairs, dtype=O.PAIR_DTYPE)
+    pairs["row"] = rng.integers(0, len(ms), npairs)
+    pairs["col"] = len(ms) + rng.integers(0, len(ns), npairs)
+    pairs["count"] = 1
+    single = np.zeros(len(ms), dtype=O.PAIR_DTYPE)
+    single["row"] = np.arange(len(ms))
+    single["col"] = len(ms) + 3
+    single["count"] = 1
+    codes = O.encode(bytes(w.ascii))
+    for tie in (0, 3):
+        cfg = capi.config(mode, tie=tie)
+        ctx = capi.Context(cfg)
+        ctx.set_seqs(0, w.ascii, w.offs)
+        ctx.share_row_seqs()
+        ctx.set_tuning(dp_traceback=3)
+        for pp in (pairs, single):
+            got = ctx.align(pp)
+            exp = O.batch(mode, codes, w.offs, codes, w.offs, pp, oracle_params(O, cfg))
+            assert_same(got, exp, pp)
+        ctx.close()
 
 
 @pytest.mark.parametrize("mode", [0, 1])
@@ -425,7 +473,7 @@ def test_checked_16bit_regions(native, oracle_mod, mode):
     ctx = capi.Context(cfg)
     ctx.set_seqs(0, ascii_, offs)
     ctx.share_row_seqs()
-    assert ctx.get_tuning().dp_traceback == 2
+    assert ctx.get_tuning().dp_traceback == 3
     got = ctx.align(pairs)
     O = oracle_mod
     codes = O.encode(bytes(ascii_))
