@@ -11,7 +11,7 @@
 
 namespace pg {
 
-// lets k_ga_dir / k_sw_dir / k_ga_pair / k_sw_pair take DIR16_DYN_SMEM of dynamic shared memory
+// lets k_ga_dir / k_ga_pair / k_sw_dir take DIR16_DYN_SMEM of dynamic shared memory
 cudaError_t dir_set_attributes();
 // bytes[t] = direction bytes of task t (bucket position), bytes[n] = 0;
 // *nchk += the checked 16-bit regions among them
@@ -21,7 +21,8 @@ void dir_sizes(bool xdrop, const KParams &kp, uint64_t *bytes, unsigned long lon
 void dir_chunk_end(const uint64_t *doff, uint64_t t0, uint64_t n, uint64_t budget, uint64_t *t1,
                    cudaStream_t st);
 // DP of the tasks [t0, t1) (grid blocks, dyn bytes of dynamic shared memory),
-// with kp.dir16_pair a pass over their half-warp regions, with chk a pass over
+// with kp.dir16_pair (X-drop) a pass over their half-warp regions (SW runs
+// them in its common pass), with chk a pass over
 // their checked 16-bit regions (each of these with its work counter
 // kp.counter[0] reset first), then their traceback (grid_tb blocks of 256
 // threads); returns the kernels launched

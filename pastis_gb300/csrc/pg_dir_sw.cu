@@ -8,14 +8,12 @@ namespace pg {
 
 cudaError_t dir_set_attributes_sw()
 {
-    const void *k[12] = {(const void *)k_sw_dir<0, false>, (const void *)k_sw_dir<1, false>,
-                         (const void *)k_sw_dir<2, false>, (const void *)k_sw_dir<3, false>,
-                         (const void *)k_sw_dir<0, true>, (const void *)k_sw_dir<1, true>,
-                         (const void *)k_sw_dir<2, true>, (const void *)k_sw_dir<3, true>,
-                         (const void *)k_sw_pair<0>, (const void *)k_sw_pair<1>,
-                         (const void *)k_sw_pair<2>, (const void *)k_sw_pair<3>};
+    const void *k[8] = {(const void *)k_sw_dir<0, false>, (const void *)k_sw_dir<1, false>,
+                        (const void *)k_sw_dir<2, false>, (const void *)k_sw_dir<3, false>,
+                        (const void *)k_sw_dir<0, true>, (const void *)k_sw_dir<1, true>,
+                        (const void *)k_sw_dir<2, true>, (const void *)k_sw_dir<3, true>};
     cudaError_t e = cudaSuccess;
-    for (int i = 0; i < 12 && e == cudaSuccess; ++i)
+    for (int i = 0; i < 8 && e == cudaSuccess; ++i)
         e = cudaFuncSetAttribute(k[i], cudaFuncAttributeMaxDynamicSharedMemorySize, DIR16_DYN_SMEM);
     return e;
 }
@@ -33,28 +31,11 @@ static void dp_sw(int tie, const KParams &kp, uint64_t t0, uint64_t t1, const ui
     }
 }
 
-static void pair_sw(int tie, const KParams &kp, uint64_t t0, uint64_t t1, const uint64_t *doff,
-                    uint8_t *arena, int *dsc, int grid, int dyn, cudaStream_t st)
-{
-    const dim3 blk(WARPS * 32);
-    switch (tie) {
-    case 0: k_sw_pair<0><<<grid, blk, dyn, st>>>(kp, t0, t1, doff, arena, dsc); break;
-    case 1: k_sw_pair<1><<<grid, blk, dyn, st>>>(kp, t0, t1, doff, arena, dsc); break;
-    case 2: k_sw_pair<2><<<grid, blk, dyn, st>>>(kp, t0, t1, doff, arena, dsc); break;
-    default: k_sw_pair<3><<<grid, blk, dyn, st>>>(kp, t0, t1, doff, arena, dsc); break;
-    }
-}
-
 int dir_run_sw(int tie, const KParams &kp, uint64_t t0, uint64_t t1, const uint64_t *doff,
                uint8_t *arena, int *dsc, int grid, int dyn, int grid_tb, bool chk, cudaStream_t st)
 {
     int launches = 2;
-    dp_sw<false>(tie, kp, t0, t1, doff, arena, dsc, grid, dyn, st);
-    if (kp.dir16_pair) {
-        cudaMemsetAsync(kp.counter, 0, sizeof(unsigned int), st);
-        pair_sw(tie, kp, t0, t1, doff, arena, dsc, grid, dyn, st);
-        ++launches;
-    }
+    dp_sw<false>(tie, kp, t0, t1, doff, arena, dsc, grid, dyn, st);   // with the half-warp pairs
     if (chk) {
         cudaMemsetAsync(kp.counter, 0, sizeof(unsigned int), st);
         dp_sw<true>(tie, kp, t0, t1, doff, arena, dsc, grid, dyn, st);

@@ -293,8 +293,8 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_ga_dir(const KParams kp, uint
 
 // DP of the half-warp regions (dir16_paired) of the tasks [t0, t1), two per
 // warp: a region waits for a partner of the same rows per lane, and those left
-// without one when the queue runs dry run alone.  Its own kernel: next to the
-// whole-warp DP in one kernel, the whole-warp loop measured 26 % slower.
+// without one when the queue runs dry run alone.  A kernel of its own: with
+// both in k_ga_dir, its whole-warp regions ran 26 % slower.
 template <int TIE>
 __global__ void __launch_bounds__(WARPS * 32, 2) k_ga_pair(const KParams kp, uint64_t t0, uint64_t t1,
                                                           const uint64_t *doff, uint8_t *arena, int *dsc)
@@ -499,7 +499,11 @@ __device__ __forceinline__ void sw_pair(const KParams &kp, int R, uint64_t a1, u
 }
 
 // local DP of the tasks [t0, t1); dsc[4p ..] = score, end row, end column,
-// have | 2 if a checked 16-bit region was redone on 32-bit lanes
+// have | 2 if a checked 16-bit region was redone on 32-bit lanes.  The
+// half-warp pairs (dir16_paired) run here too, two per warp: a pair waits for
+// a partner of the same rows per lane, and those left without one run alone
+// at the end.  (A pass of their own, as X-drop's k_ga_pair, measured 5 %
+// slower here: sw100k is 10 ms, and a second pass adds a second tail.)
 template <int TIE, bool CHK>
 __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint64_t t0, uint64_t t1,
                                                       const uint64_t *doff, uint8_t *arena, int *dsc)
@@ -514,6 +518,7 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint
     unsigned long long exec = 0;
     const uint64_t base = doff[t0];
     WarpQueue q;
+    PairSlots slots;
     uint64_t u;
     while (q.pop(&kp.counter[CHK ? 0 : 3], t1 - t0, u)) {
         const uint64_t t = t0 + u;
@@ -524,8 +529,14 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint
         int m, n;
         if (!pair_seqs(kp, pr, V, m, Hs, n)) continue;
         if ((dir16_mode(kp, m, n) == 2) != CHK) continue;   // this pass's pairs only
-        if (!CHK && dir16_paired(kp, m, n)) continue;        // k_sw_pair's
         exec += (unsigned long long)m * (unsigned long long)n;
+        if (!CHK && dir16_paired(kp, m, n)) {
+            // half a warp: wait for a partner of the same rows per lane
+            const int R = dir16_pair_rows(m);
+            const uint64_t w1 = slots.swap(R, u + 1);
+            if (w1) sw_pair<TIE>(kp, R, w1, u + 1, t0, doff, base, arena, ssm, prof, dsc);
+            continue;
+        }
         DirOut d;
         d.score = 0; d.ei = 0; d.ej = 0; d.have = 0;
         if (m > 0 && n > 0)
@@ -536,52 +547,13 @@ __global__ void __launch_bounds__(WARPS * 32, 2) k_sw_dir(const KParams kp, uint
             *o = make_int4(d.score, d.ei, d.ej, d.have | (d.sat << 1));
         }
     }
-    if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
-}
-
-// local DP of the half-warp pairs (dir16_paired) of the tasks [t0, t1), two
-// per warp, as k_ga_pair
-template <int TIE>
-__global__ void __launch_bounds__(WARPS * 32, 2) k_sw_pair(const KParams kp, uint64_t t0, uint64_t t1,
-                                                          const uint64_t *doff, uint8_t *arena, int *dsc)
-{
-    __shared__ int ssm[32 * 32];
-    load_sm(ssm, kp.sm);
-    __syncthreads();
-    uint2 *prof = dir_prof(kp);
-    const int lane = threadIdx.x & 31;
-    unsigned long long exec = 0;
-    const uint64_t base = doff[t0];
-    WarpQueue q;
-    PairSlots slots;
-    // one call site of the DP, as in k_ga_pair
-    int flush = 0;
-    for (;;) {
-        uint64_t a1 = 0, b1 = 0;
-        int R = 0;
-        if (flush == 0) {
-            uint64_t u;
-            if (!q.pop(&kp.counter[0], t1 - t0, u)) { flush = 1; continue; }
-            const uint64_t t = t0 + u;
-            const uint64_t p = kp.order ? (uint64_t)kp.order[t] : t;
-            if (p >= kp.n) continue;
-            const pg_pair pr = kp.pairs[p];
-            const uint8_t *V, *Hs;
-            int m, n;
-            if (!pair_seqs(kp, pr, V, m, Hs, n)) continue;
-            if (!dir16_paired(kp, m, n)) continue;
-            exec += (unsigned long long)m * (unsigned long long)n;
-            R = dir16_pair_rows(m);
-            b1 = u + 1;
-            a1 = slots.swap(R, b1);
-            if (!a1) continue;
-        } else {
-            if (flush > 8) break;
-            R = flush++;
-            a1 = __shfl_sync(FULL, slots.pend, R);
-            if (!a1) continue;
+    if (!CHK && kp.dir16_pair) {
+        // pairs left without a partner run on half a warp alone
+#pragma unroll 1
+        for (int R = 1; R <= 8; ++R) {
+            const uint64_t w1 = __shfl_sync(FULL, slots.pend, R);
+            if (w1) sw_pair<TIE>(kp, R, w1, 0, t0, doff, base, arena, ssm, prof, dsc);
         }
-        sw_pair<TIE>(kp, R, a1, b1, t0, doff, base, arena, ssm, prof, dsc);
     }
     if (lane == 0 && exec) atomicAdd(kp.exec_cells + 1, exec);
 }

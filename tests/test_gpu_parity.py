@@ -45,9 +45,9 @@ def run_both(mode, w, cfg, O, pairs=None, roff=0, coff=0, share=True):
     got = ctx.align(pairs, roff, coff)
     # traceback form by default: X-drop: k_xdf, k_xd_wide, k_hist, k_bucket,
     # k_dirsize, k_ga_dir, k_ga_pair, k_tb_ga; SW: k_hist, k_bucket, k_dirsize,
-    # k_sw_dir, k_sw_pair, k_tb_sw; one more (the checked 16-bit pass) where
-    # long regions need it
-    base = 8 if mode == capi.MODE_XDROP else 6
+    # k_sw_dir, k_tb_sw; one more (the checked 16-bit pass) where long regions
+    # need it
+    base = 8 if mode == capi.MODE_XDROP else 5
     assert ctx.last_launches() in (base, base + 1)
     codes = O.encode(bytes(ascii_))
     exp = O.batch(mode, codes, w.offs, codes, w.offs, pairs, oracle_params(O, cfg),
