@@ -323,7 +323,7 @@ def run_gpu(args, rank, world, local_rank):
                      1: "k_ga_dir + k_tb_ga" if mode else "k_sw_dir + k_tb_sw",
                      2: ("k_ga_dir + k_tb_ga" if mode else "k_sw_dir + k_tb_sw")
                      + " (16-bit lanes)",
-                     3: ("k_ga_dir + k_tb_ga" if mode else "k_sw_dir + k_tb_sw")
+                     3: ("k_ga_dir + k_ga_pair + k_tb_ga" if mode else "k_sw_dir + k_tb_sw")
                      + " (16-bit lanes, two regions per warp)"}[form]
         tpath = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tpath):
