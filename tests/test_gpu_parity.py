@@ -291,6 +291,8 @@ def test_tuning_and_graph_replay_keep_results(native, oracle_mod, mode):
         ctx.set_tuning(rows_max=9)
     with pytest.raises(capi.PgError):
         ctx.set_tuning(graph=2)
+    with pytest.raises(capi.PgError):
+        ctx.set_tuning(dp_traceback=4)
     ctx.close()
 
 
@@ -415,13 +417,15 @@ def test_pair_form_row_boundaries(native, oracle_mod, mode):
         ctx.close()
 
 
+@pytest.mark.parametrize("form", [2, 3])
 @pytest.mark.parametrize("mode", [0, 1])
 @pytest.mark.parametrize("scale", [8, 10])
-def test_traceback16_limit_splits_the_batch(sw_small, xd_small, oracle_mod, mode, scale):
+def test_traceback16_limit_splits_the_batch(sw_small, xd_small, oracle_mod, mode, scale, form):
     """A substitution table scaled by 8 (largest magnitude 88) leaves 16-bit
     lanes only to regions with m + n <= 336, so one batch runs on both lane
-    widths; scaled by 10 (magnitude 110) no region qualifies.  Results equal
-    the oracle's run with the same table."""
+    widths; scaled by 10 (magnitude 110) no region qualifies.  Forms 2 and 3
+    (form 3 puts the short 16-bit regions two per warp).  Results equal the
+    oracle's run with the same table."""
     from pastis_gb300 import capi
     O = oracle_mod
     w = sw_small if mode == capi.MODE_SW else xd_small
@@ -431,7 +435,7 @@ def test_traceback16_limit_splits_the_batch(sw_small, xd_small, oracle_mod, mode
     ctx = capi.Context(cfg)
     ctx.set_seqs(0, w.ascii, w.offs)
     ctx.share_row_seqs()
-    ctx.set_tuning(dp_traceback=2)
+    ctx.set_tuning(dp_traceback=form)
     got = ctx.align(w.pairs)
     codes = O.encode(bytes(w.ascii))
     first, ext, xg = capi.resolved_gaps(cfg)
