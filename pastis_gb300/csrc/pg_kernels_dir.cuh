@@ -1,8 +1,10 @@
 // pg_kernels_dir.cuh -- the traceback form of the alignment kernels (tuning
 // option dp_traceback): k_ga_dir / k_sw_dir run dp_warp_dir, or dp_warp_dir16
 // on 16-bit lanes for the regions that fit them (dp_traceback 2; one warp per
-// region, direction nibbles into an HBM arena), k_tb_ga / k_tb_sw trace them
-// back (one thread per pair, pg_trace.cuh) and write the same pg_result records k_ga /
+// region, direction nibbles into an HBM arena); with dp_traceback 3 the 16-bit
+// regions of up to 256 rows run two per warp in dp_pair_dir16 (X-drop: in
+// k_ga_pair, SW: inside k_sw_dir).  k_tb_ga / k_tb_sw trace them back (one
+// thread per pair, pg_trace.cuh) and write the same pg_result records k_ga /
 // k_sw write.  A batch whose direction matrices exceed the arena runs in
 // chunks of consecutive tasks (bucket order), each chunk DP then traceback.
 #pragma once
