@@ -7,13 +7,26 @@ synthetic candidate pairs from 200k proteins (lognormal lengths, median 250,
 clamp 30-1000; half homologs at 30-80 % identity), BLOSUM62 with PASTIS's gap
 parameters -11 / -2.  A step is one pass of the aligner over the whole batch.
 
-  value  GCUPS with inputs resident in HBM (device buffers, pg_align_device)
-  e2e    GCUPS through pg_align with pinned host buffers: pair upload and
-         result download inside the timed region
+  value           GCUPS with inputs resident in HBM (device buffers,
+                  pg_align_device), algorithmic cells (both seeds in full)
+  executed_gcups  the cells the kernels computed (a repeated seed or region
+                  is not recomputed) over the same time
+  e2e             GCUPS through pg_align with pinned host buffers: pair upload
+                  and result download inside the timed region
+  parity          the oracle's results for the cpu_baseline sample (and up to
+                  --parity-pairs pairs) against the GPU's, every byte of every
+                  pg_result
+  workloads       the sw100k Smith-Waterman batch (plain and filtered) measured
+                  in the same run
+
+With --gpus N (torchrun) every rank aligns its Sum(m*n)-balanced range of an
+N-times larger batch over the same proteins (pastis_gb300/shard.py): weak
+scaling, no collective on the data path.
 
 --impl reference times the CPU restatement of the reference's SeqAn path
 (the oracle; SeqAn itself is absent from the reference checkout) on all host
-cores, on a bounded sample of the same workload.
+cores.  It maps no library of this package but the synthetic generator: each
+timed step aligns the next window of the same batch, wrapping around.
 """
 import argparse
 import json
@@ -22,15 +35,17 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "GCUPS & alignments/s, batched SW/X-drop: GPU plain vs tuned+filtered vs CPU"
-DPX_OPS_PER_CELL = 4  # E, F, H add-max and the max with the third term, int32
-SW_WORKLOADS = ("sw100k", "filter5m")
+# roofline model: E, F and H as add-max DPX-class ops plus the max with the
+# third term, per cell on 32-bit lanes
+DPX_OPS_PER_CELL = 4
+SW_WORKLOADS = ("sw100k", "filter5m", "uneven10m_sw")
+SEED = 20260101
 
 
 def parse():
@@ -40,17 +55,23 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="xdrop1m",
-                    choices=["xdrop1m", "sw100k", "uneven10m", "filter5m", "manytomany"])
+                    choices=["xdrop1m", "sw100k", "uneven10m", "uneven10m_sw", "filter5m",
+                             "manytomany"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="CPU work per baseline sample (seconds)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--parity-pairs", type=int, default=300_000,
+                    help="pairs of the timed batch checked against the oracle (at least the "
+                         "cpu_baseline sample)")
     ap.add_argument("--set-tuning", default="",
                     help="launch tuning of the plain arm, e.g. dp_traceback=0,bucket_order=1")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuned arm (tuned)")
     ap.add_argument("--no-filter", action="store_true",
                     help="skip the learned-filter arm (tuned_filtered)")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="skip the sw100k record of the default run")
     ap.add_argument("--filter-train-frac", type=float, default=0.5,
                     help="training batch size as a fraction of the timed batch")
     ap.add_argument("--blocks", type=int, default=4,
@@ -62,7 +83,7 @@ def parse():
     return ap.parse_args()
 
 
-def workload_desc(name, n, scale):
+def workload_desc(name, n, nseqs):
     base = {
         "xdrop1m": "seeded X-drop (x=49, k=6, <=2 seeds) + global alignment + stats + "
                    "coverage/ANI filter, %d candidate pairs over %d synthetic proteins "
@@ -71,14 +92,46 @@ def workload_desc(name, n, scale):
         "sw100k": "affine Smith-Waterman + stats + coverage/ANI filter, %d pairs over %d "
                   "synthetic proteins (lognormal lengths median 250 clamp 30-1000)",
         "uneven10m": "seeded X-drop, %d pairs over %d proteins, lengths 80%% lognormal "
-                     "median 300 + 20%% uniform 1000-5000",
+                     "median 300 + 20%% uniform 1000-5000, min 20",
+        "uneven10m_sw": "affine Smith-Waterman + stats + coverage/ANI filter, %d pairs over %d "
+                        "proteins, lengths 80%% lognormal median 300 + 20%% uniform 1000-5000, "
+                        "min 20",
         "filter5m": "affine Smith-Waterman + stats + coverage/ANI filter, %d pairs over %d "
                     "synthetic proteins (lognormal lengths median 250 clamp 30-1000, 30%% "
                     "homologs)",
     }[name]
+    return base % (n, nseqs)
+
+
+def mode_of(workload):
+    return 0 if workload in SW_WORKLOADS else 1
+
+
+def line_config(args, n, nseqs, world):
+    """The config record both arms print (the same dict for the same run)."""
+    mode = mode_of(args.workload)
+    return {"workload": args.workload + ": " + workload_desc(args.workload, n, nseqs),
+            "mode": "xdrop" if mode else "sw", "pairs": n,
+            "scoring": "BLOSUM62; gap_open -11, gap_ext -2 given to the score model in SeqAn's "
+                       "constructor order, as PASTIS calls it",
+            "l2": "GPU arm: flushed between timed steps (512 MiB write, outside the timed "
+                  "region)",
+            "parallelism": "dp%d: each rank aligns its Sum(m*n)-balanced range of a %d-rank "
+                           "batch (independent pairs, no collective)" % (world, world)}
+
+
+def rank_batch(workload, scale, rank, world):
+    """This rank's pairs: a batch of world x the preset's pairs over the same
+    proteins, cut into Sum(m*n)-balanced contiguous ranges (shard.py).  At one
+    rank it is the preset's batch."""
     from pastis_gb300 import synth
-    p = synth.PRESETS[name]
-    return base % (n, int(round(p["nseqs"] * scale)))
+    from pastis_gb300.shard import my_range, pair_cost
+    npairs = synth.PRESETS[workload]["npairs"] * world
+    w = synth.generate(workload, seed=SEED, scale=scale, npairs=npairs)
+    if world == 1:
+        return w
+    b, e = my_range(pair_cost(w.pairs, w.lengths()), rank, world)
+    return w.subset(slice(b, e))
 
 
 class Clocks:
@@ -99,7 +152,7 @@ class Clocks:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -129,10 +182,16 @@ class Clocks:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_sample(w, mode, p, budget_s, threads):
-    """Oracle over a prefix of the pairs sized to about budget_s of CPU time."""
+def oracle_codes(w):
     from oracle import oracle as O
-    codes = O.encode(bytes(w.ascii))
+    return O.encode(bytes(w.ascii))
+
+
+def cpu_sample(w, mode, p, budget_s, threads, codes=None):
+    """Oracle over a prefix of the pairs sized to about budget_s of CPU time.
+    Returns (cells, pairs, seconds, results)."""
+    from oracle import oracle as O
+    codes = oracle_codes(w) if codes is None else codes
     n = min(len(w.pairs), 500)
     while True:
         t = time.perf_counter()
@@ -140,17 +199,34 @@ def cpu_sample(w, mode, p, budget_s, threads):
         dt = time.perf_counter() - t
         if dt >= budget_s * 0.5 or n >= len(w.pairs):
             cells = int(out["cells"].astype(np.uint64).sum())
-            return cells, n, dt
+            return cells, n, dt, out
         n = min(len(w.pairs), int(n * max(2.0, budget_s / max(dt, 1e-3) * 0.9)))
 
 
-def oracle_params(cfg):
+def parity_record(got, exp, what):
+    """Byte comparison of every pg_result field of the GPU's results with the
+    oracle's for the same pairs."""
+    g = np.ascontiguousarray(got).view(np.uint8).reshape(len(got), -1)
+    e = np.ascontiguousarray(exp).view(np.uint8).reshape(len(exp), -1)
+    bad = (g != e).any(axis=1)
+    per = {}
+    for f in exp.dtype.names:
+        a = np.ascontiguousarray(got[f]).view(np.uint8).reshape(len(got), -1)
+        b = np.ascontiguousarray(exp[f]).view(np.uint8).reshape(len(exp), -1)
+        k = int((a != b).any(axis=1).sum())
+        if k:
+            per[f] = k
+    return {"pairs_checked": int(len(got)), "mismatches": int(bad.sum()),
+            "fields": list(exp.dtype.names), "field_mismatches": per,
+            "compare": "raw bytes of every pg_result field (f32 identity and score_aln as bit "
+                       "patterns)", "pairs": what}
+
+
+def oracle_params_for(mode):
+    """The oracle's parameters for this bench's configuration: PASTIS's
+    defaults in SeqAn's constructor order (pg_config_default's)."""
     from oracle import oracle as O
-    from pastis_gb300 import capi
-    first, ext, xg = capi.resolved_gaps(cfg)
-    return O.make_params(gap_first=first, gap_ext=ext, xdrop_gap=xg, xdrop=cfg.xdrop,
-                         seed_len=cfg.seed_len, seed_count=cfg.seed_count, tie=cfg.tie,
-                         flags=cfg.flags, cov_thr=cfg.cov_thr, ani_thr=cfg.ani_thr)
+    return O.pastis_params(as_called=True)
 
 
 def host_cores():
@@ -160,53 +236,82 @@ def host_cores():
         return os.cpu_count() or 1
 
 
-def run_reference(args, rank):
-    """CPU restatement of the reference path, all host cores, bounded sample per step."""
+def run_reference(args, rank, world):
+    """CPU restatement of the reference path on all host cores.  Each timed
+    step aligns the next window of the batch (wrapping), sized so that the
+    whole run takes a few minutes; GCUPS = cells of all timed windows / their
+    time."""
     from oracle import oracle as O
-    from pastis_gb300 import capi, synth
+    from pastis_gb300 import build
     if rank != 0:
         return
+    build.build(only={"libpastis_synth.so"})
     O.build()
-    w = synth.generate(args.workload, seed=20260101, scale=args.scale)
-    mode = capi.MODE_SW if args.workload in SW_WORKLOADS else capi.MODE_XDROP
-    cfg = capi.config(mode)
-    p = oracle_params(cfg)
+    w = rank_batch(args.workload, args.scale, 0, world)
+    N = len(w.pairs)
+    mode = mode_of(args.workload)
+    p = oracle_params_for(mode)
     cores = host_cores()
-    # size one step to about 10 s of CPU time
-    cells, n, dt = cpu_sample(w, mode, p, 10.0, cores)
-    codes = O.encode(bytes(w.ascii))
-    sub = w.pairs[:n]
-    for _ in range(args.warmup):
-        O.batch(mode, codes, w.offs, codes, w.offs, sub[:max(1, n // 10)], p, nthreads=cores)
+    codes = oracle_codes(w)
+    # window size: about 150 s for the whole run, 2 to 10 s per step
+    per_step = min(10.0, max(2.0, 150.0 / max(1.0, args.steps + 0.2 * args.warmup)))
+    _, ns, _, _ = cpu_sample(w, mode, p, per_step, cores, codes)
+    ns = max(1, min(ns, N))
+
+    def window(k):
+        b = (k * ns) % N
+        idx = np.arange(b, b + ns) % N
+        return w.pairs[idx]
+
+    for k in range(args.warmup):
+        sub = window(k)
+        O.batch(mode, codes, w.offs, codes, w.offs, sub[:max(1, ns // 10)], p, nthreads=cores)
+    cells = 0
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        out = O.batch(mode, codes, w.offs, codes, w.offs, sub, p, nthreads=cores)
+    for k in range(args.steps):
+        out = O.batch(mode, codes, w.offs, codes, w.offs, window(k), p, nthreads=cores)
+        cells += int(out["cells"].astype(np.uint64).sum())
     dt = time.perf_counter() - t0
-    cells = int(out["cells"].astype(np.uint64).sum())
-    gcups = cells * args.steps / dt / 1e9
-    sample = "first %d of %d pairs of the workload per step" % (n, len(w.pairs))
+    gcups = cells / dt / 1e9
+    covered = min(N, ns * args.steps)
+    sample = ("each step aligns the next %d of the batch's %d pairs (wrapping), %d distinct "
+              "pairs over the %d timed steps; the reference's SeqAn path cannot be built "
+              "(empty submodules), the oracle restates it" % (ns, N, covered, args.steps))
     line = {
         "metric": METRIC, "value": gcups, "unit": "GCUPS", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic",
-        "config": {"workload": args.workload + ": " + workload_desc(args.workload, len(w.pairs),
-                                                                    args.scale),
-                   "mode": "xdrop" if mode else "sw", "pairs_per_step": n},
+        "config": line_config(args, N, int(len(w.offs) - 1), world),
         "impl": "reference",
-        "alignments_per_s": n * args.steps / dt,
+        "alignments_per_s": ns * args.steps / dt,
+        "pairs_per_step": ns,
         "cpu_baseline": {"value": gcups, "unit": "GCUPS", "cores": cores, "kind": "port",
-                         "sample": sample + "; the reference's SeqAn path cannot be built "
-                                            "(empty submodules), the oracle restates it"},
+                         "sample": sample},
         "e2e": {"value": gcups, "unit": "GCUPS", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
+def time_steps(step, stream, flush, steps):
+    """CUDA-event time (ms) of each of `steps` calls of step() on `stream`,
+    L2 flushed before each, outside the timed window."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    for k in range(steps):
+        flush.fill_(k & 0xff)
+        ev[k][0].record(stream)
+        step()
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
 def run_gpu(args, rank, world, local_rank):
     import torch
-    from pastis_gb300 import capi, synth
+    from pastis_gb300 import capi
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -214,9 +319,8 @@ def run_gpu(args, rank, world, local_rank):
         dist.init_process_group("nccl")
     dev = local_rank
     torch.cuda.set_device(dev)
-    mode = capi.MODE_SW if args.workload in SW_WORKLOADS else capi.MODE_XDROP
-    # weak scaling: every rank aligns its own batch of the same shape
-    w = synth.generate(args.workload, seed=20260101 + rank, scale=args.scale)
+    mode = mode_of(args.workload)
+    w = rank_batch(args.workload, args.scale, rank, world)
     n = len(w.pairs)
     cfg = capi.config(mode, device=dev)
     ctx = capi.Context(cfg)
@@ -276,13 +380,17 @@ def run_gpu(args, rank, world, local_rank):
     exec_cells = exec_xd + exec_dp
     dp_ms = kern_ms[1] / args.steps
     xd_ms = kern_ms[0] / args.steps
+    tot = torch.tensor([total_ms, float(alg_cells), float(exec_cells), float(n)],
+                       dtype=torch.float64, device=f"cuda:{dev}")
     if dist is not None:
-        t = torch.tensor([total_ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        mx = tot[:1].clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tot)
+        tot[0] = mx[0]
+    total_ms, all_cells, all_exec, all_pairs = (float(x) for x in tot.tolist())
     ms_step = total_ms / args.steps
-    gcups = alg_cells * world / (ms_step * 1e-3) / 1e9
-    aln_s = n * world / (ms_step * 1e-3)
+    gcups = all_cells / (ms_step * 1e-3) / 1e9
+    aln_s = all_pairs / (ms_step * 1e-3)
 
     # end to end: pinned host pairs in, results out, through pg_align
     h_pairs = torch.empty(n * capi.PAIR_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
@@ -305,7 +413,7 @@ def run_gpu(args, rank, world, local_rank):
         t = torch.tensor([e2e_s], device=f"cuda:{dev}", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    e2e_gcups = alg_cells * world / e2e_s / 1e9
+    e2e_gcups = all_cells / e2e_s / 1e9
     same = bool((ov.view(np.uint8) == res.view(np.uint8)).all())
 
     line = None
@@ -316,7 +424,7 @@ def run_gpu(args, rank, world, local_rank):
         # bounds twice the cells (the conservative peak for a mixed batch)
         cells_per_op = 2 if form >= 2 else 1
         peak_gcups = peak_ops * cells_per_op / DPX_OPS_PER_CELL / 1e9
-        # dominant kernel: the alignment DP (k_ga / k_sw), its own cells and time
+        # dominant kernel: the alignment DP and its traceback, executed cells
         achieved = exec_dp / (dp_ms * 1e-3) / 1e9
         traffic = None
         dp_kernel = {0: "k_ga" if mode else "k_sw",
@@ -339,26 +447,30 @@ def run_gpu(args, rank, world, local_rank):
         alg_bytes = int((lens[w.pairs["row"]] + lens[w.pairs["col"]]).sum()) + n * (
             capi.PAIR_DTYPE.itemsize + capi.RESULT_DTYPE.itemsize)
         hbm_gbs = alg_bytes / (ms_step * 1e-3) / 1e9
+        if form >= 2:
+            peak_src = ("measured %.4g DPX add-max/s (pg_dpx_peak, int32) / %d DPX-class ops "
+                        "per cell x 2 cells per packed 16-bit op (model; the 16-bit kernels "
+                        "issue max/add.s16x2, not add-max)" % (peak_ops, DPX_OPS_PER_CELL))
+        else:
+            peak_src = ("measured %.4g DPX add-max/s (pg_dpx_peak, int32) / %d DPX-class ops "
+                        "per cell (model)" % (peak_ops, DPX_OPS_PER_CELL))
         line = {
             "metric": METRIC, "value": gcups, "unit": "GCUPS", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32", "data": "synthetic",
-            "config": {"workload": args.workload + ": " + workload_desc(args.workload, n,
-                                                                        args.scale),
-                       "mode": "xdrop" if mode else "sw", "pairs": n,
-                       "scoring": "BLOSUM62; gap_open -11, gap_ext -2 given to the score "
-                                  "model in SeqAn's constructor order, as PASTIS calls it",
-                       "l2": "flushed between timed steps (512 MiB write, outside the "
-                             "timed region)",
-                       "parallelism": "dp%d (independent pair batches per GPU)" % world},
+            "config": line_config(args, n, int(len(w.offs) - 1), world),
             "alignments_per_s": aln_s,
+            "executed_gcups": all_exec / (ms_step * 1e-3) / 1e9,
+            "cells_note": "value counts algorithmic cells (both seeds in full, the CPU "
+                          "baseline's definition); executed_gcups the cells the kernels "
+                          "computed",
             "algorithmic_cells_per_step": alg_cells,
             "executed_cells_per_step": exec_cells,
             "gpu_launches": launches,
             "clocks": clk,
             "e2e": {"value": e2e_gcups, "unit": "GCUPS",
-                    "alignments_per_s": n * world / e2e_s,
+                    "alignments_per_s": all_pairs / e2e_s,
                     "h2d_bytes_per_step": n * capi.PAIR_DTYPE.itemsize,
                     "d2h_bytes_per_step": n * capi.RESULT_DTYPE.itemsize,
                     "matches_device_run": same},
@@ -368,11 +480,7 @@ def run_gpu(args, rank, world, local_rank):
                          "unit": "GCUPS", "frac": achieved / peak_gcups, "traffic": traffic,
                          "kernel": dp_kernel,
                          "kernel_ms": dp_ms, "kernel_cells": exec_dp,
-                         "peak_source": "measured %.4g DPX add-max/s (pg_dpx_peak) / %d "
-                                        "DPX ops per cell%s" % (
-                                            peak_ops, DPX_OPS_PER_CELL,
-                                            ", x 2 cells per packed 16-bit op" if form == 2
-                                            else " (int32)"),
+                         "peak_source": peak_src,
                          "hbm": {"achieved_GBps": hbm_gbs,
                                  "peak_GBps": peaks.get("hbm_gbs"),
                                  "frac": hbm_gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs")
@@ -381,26 +489,93 @@ def run_gpu(args, rank, world, local_rank):
                                          "the pair record and the result per pair"}},
             "wall_s_timed": t_wall,
         }
+        if mode == 1 and xd_ms > 0:
+            line["extension"] = {"kernel_ms": xd_ms, "executed_cells": exec_xd,
+                                 "executed_gcups": exec_xd / (xd_ms * 1e-3) / 1e9}
     if rank == 0 and not args.no_tune:
         line["tuned"] = tuned_arm(args, w, ctx, mode, dev, stream, flush, d_pairs, res, ms_step)
     if rank == 0 and not args.no_filter:
-        line["tuned_filtered"] = filtered_arm(args, w, ctx, dev, stream, flush, d_pairs, res,
-                                              ms_step)
+        line["tuned_filtered"] = filtered_arm(args.workload, args, w, ctx, dev, stream, flush,
+                                              d_pairs, res, ms_step)
         line["tuned_filtered"]["tuning"] = ctx.get_tuning().as_dict()
-    if not args.no_cpu_baseline and rank == 0:
+    if rank == 0:
         cores = host_cores()
-        p = oracle_params(cfg)
-        cells, ns, dt = cpu_sample(w, mode, p, args.cpu_seconds, cores)
-        line["cpu_baseline"] = {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": cores,
-                                "kind": "port",
-                                "sample": "first %d of %d pairs (%.3g cells) in %.1f s" % (
-                                    ns, n, cells, dt),
-                                "alignments_per_s": ns / dt}
+        p = oracle_params_for(mode)
+        codes = oracle_codes(w)
+        exp = None
+        if not args.no_cpu_baseline:
+            cells, ns, dt, exp = cpu_sample(w, mode, p, args.cpu_seconds, cores, codes)
+            line["cpu_baseline"] = {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": cores,
+                                    "kind": "port",
+                                    "sample": "first %d of %d pairs (%.3g cells) in %.1f s" % (
+                                        ns, n, cells, dt),
+                                    "alignments_per_s": ns / dt}
+        want = min(n, args.parity_pairs)
+        if exp is None:
+            exp = np.zeros(0, dtype=res.dtype)
+        if len(exp) < want:
+            from oracle import oracle as O
+            more = O.batch(mode, codes, w.offs, codes, w.offs, w.pairs[len(exp):want], p,
+                           nthreads=cores)
+            exp = np.concatenate([exp, more])
+        if len(exp):
+            line["parity"] = parity_record(res[:len(exp)], exp,
+                                           "the first %d pairs of the timed batch" % len(exp))
+    if rank == 0 and args.workload == "xdrop1m" and not args.no_workloads:
+        line["workloads"] = {"sw100k": sw100k_record(args, dev, stream, flush)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def sw100k_record(args, dev, stream, flush):
+    """The sw100k Smith-Waterman batch (100k pairs over 20k proteins) in the
+    same run: plain GCUPS, parity of every pair against the oracle, and the
+    learned filter in front of the same aligner."""
+    import torch
+    from pastis_gb300 import capi, synth
+    w = synth.generate("sw100k", seed=SEED, scale=args.scale)
+    n = len(w.pairs)
+    ctx = capi.Context(capi.config(capi.MODE_SW, device=dev))
+    ctx.set_seqs(0, w.ascii, w.offs)
+    ctx.share_row_seqs()
+    torch.cuda.set_stream(stream)
+    d_pairs = torch.from_numpy(w.pairs.view(np.uint8).copy()).to(f"cuda:{dev}")
+    d_out = torch.empty(n * capi.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{dev}")
+
+    def step():
+        ctx.align_device(d_pairs.data_ptr(), n, d_out.data_ptr(), stream.cuda_stream)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize(dev)
+    res = np.frombuffer(d_out.cpu().numpy().tobytes(), dtype=capi.RESULT_DTYPE)
+    cells = int(res["cells"].astype(np.uint64).sum())
+    e0 = ctx.exec_cells_split()
+    ms = statistics.mean(time_steps(step, stream, flush, max(args.steps, 5)))
+    e1 = ctx.exec_cells_split()
+    km = ctx.kernel_ms()
+    out = {"config": "sw100k: " + workload_desc("sw100k", n, int(len(w.offs) - 1)),
+           "value": cells / (ms * 1e-3) / 1e9, "unit": "GCUPS", "ms_per_step": ms,
+           "alignments_per_s": n / (ms * 1e-3),
+           "executed_cells_per_step": (e1[1] - e0[1]) / max(args.steps, 5),
+           "alignment_kernel_ms_last_step": km[1]}
+    if not args.no_filter:
+        out["tuned_filtered"] = filtered_arm("sw100k", args, w, ctx, dev, stream, flush, d_pairs,
+                                             res, ms)
+    from oracle import oracle as O
+    p = oracle_params_for(capi.MODE_SW)
+    codes = oracle_codes(w)
+    t0 = time.perf_counter()
+    exp = O.batch(capi.MODE_SW, codes, w.offs, codes, w.offs, w.pairs, p, nthreads=host_cores())
+    dt = time.perf_counter() - t0
+    out["parity"] = parity_record(res, exp, "every pair of the batch")
+    out["cpu_baseline"] = {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": host_cores(),
+                           "kind": "port", "sample": "all %d pairs in %.1f s" % (n, dt)}
+    ctx.close()
+    return out
 
 
 def tuned_arm(args, w, ctx, mode, dev, stream, flush, d_pairs, plain_res, plain_ms):
@@ -444,20 +619,22 @@ def tuned_arm(args, w, ctx, mode, dev, stream, flush, d_pairs, plain_res, plain_
                        "full_batch_check": rep.get("validated_on_full_batch")}}
 
 
-def filtered_arm(args, w, ctx, dev, stream, flush, d_pairs, plain_res, plain_ms):
+def filtered_arm(workload, args, w, ctx, dev, stream, flush, d_pairs, plain_res, plain_ms):
     """The learned pair filter in front of the same aligner on the same batch.
 
     A filter is trained (this library's BF16 kernels) on a separate batch of
-    the same generator, labelled by the SW kernel; its threshold keeps 99.5 %
+    the same generator, labelled by the SW kernel; its threshold keeps 99.7 %
     of the positive validation pairs.  Timed per step: features, network,
     compaction, alignment of the kept pairs, scatter of the results.  Recall
-    is measured on the timed batch itself against SW labels of every pair."""
+    is measured on the timed batch itself against SW labels of every pair.
+
+    ceiling: the same aligner on the positive pairs alone (a perfect filter,
+    with no filter cost), which bounds what any pair filter can gain here."""
     import torch
     from pastis_gb300 import capi, synth
     from pastis_gb300 import filter as F
     n = len(w.pairs)
-    wt = synth.generate(args.workload, seed=20260101 + 7919,
-                        scale=args.scale * args.filter_train_frac)
+    wt = synth.generate(workload, seed=SEED + 7919, scale=args.scale * args.filter_train_frac)
     # the threshold keeps 99.7 % of the validation positives so that the
     # recall measured on the (different) timed batch stays above 99.5 %
     f, thr, fm = F.fit(wt, dev, recall=0.997)
@@ -492,6 +669,25 @@ def filtered_arm(args, w, ctx, dev, stream, flush, d_pairs, plain_res, plain_ms)
     e1.record(stream)
     torch.cuda.synchronize(dev)
     pos = labels > 0.5
+    # the perfect filter: only the positives, already compacted on the device
+    npos = int(pos.sum())
+    ceiling = None
+    if npos:
+        d_pos = torch.from_numpy(w.pairs[pos].view(np.uint8).copy()).to(f"cuda:{dev}")
+        d_pout = torch.empty(npos * capi.RESULT_DTYPE.itemsize, dtype=torch.uint8,
+                             device=f"cuda:{dev}")
+
+        def pos_step():
+            ctx.align_device(d_pos.data_ptr(), npos, d_pout.data_ptr(), stream.cuda_stream)
+
+        for _ in range(2):
+            pos_step()
+        pms = statistics.mean(time_steps(pos_step, stream, flush, args.steps))
+        ceiling = {"ms_per_step": pms, "aligned_pairs": npos,
+                   "alignments_per_s": n / (pms * 1e-3),
+                   "vs_plain_alignments_per_s": plain_ms / pms,
+                   "note": "aligning only the pairs the label marks positive, no filter cost: "
+                           "the most any pair filter can gain on this batch"}
     out = {
         "alignments_per_s": n / (ms * 1e-3),
         "ms_per_step": ms,
@@ -512,6 +708,7 @@ def filtered_arm(args, w, ctx, dev, stream, flush, d_pairs, plain_res, plain_ms)
                      "kmer_rule_kept_at_same_recall": fm["kmer_rule_kept_at_same_recall"]},
         "alignments_per_s_counts": "candidate pairs resolved per second (pruned pairs get "
                                    "score_aln 0 and the filtered flag)",
+        "ceiling": ceiling,
     }
     f.close()
     return out
@@ -692,10 +889,10 @@ def run_manytomany(args, rank, world, local_rank):
             "end_to_end_s": {"plain": gen_s + plain_s, "tuned_filtered": gen_s + filt_s},
         }
         if not args.no_cpu_baseline:
-            p = oracle_params(cfg)
+            p = oracle_params_for(capi.MODE_XDROP)
             sub = types.SimpleNamespace(pairs=allp[rng.permutation(len(allp))], ascii=w.ascii,
                                         offs=w.offs)
-            c, n, dt = cpu_sample(sub, capi.MODE_XDROP, p, args.cpu_seconds, host_cores())
+            c, n, dt, _ = cpu_sample(sub, capi.MODE_XDROP, p, args.cpu_seconds, host_cores())
             line["cpu_baseline"] = {"value": c / dt / 1e9, "unit": "GCUPS", "cores": host_cores(),
                                     "kind": "port", "sample": "%d random candidate pairs in "
                                                               "%.1f s" % (n, dt),
@@ -711,11 +908,12 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
     from pastis_gb300 import build
     build.build()
-    if args.impl == "reference":
-        run_reference(args, rank)
-    elif args.workload == "manytomany":
+    if args.workload == "manytomany":
         run_manytomany(args, rank, world, local_rank)
     else:
         run_gpu(args, rank, world, local_rank)

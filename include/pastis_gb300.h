@@ -30,7 +30,6 @@ extern "C" {
 #define PG_ERR_ARG      -1   /* bad argument (null pointer, size, index, option) */
 #define PG_ERR_CUDA     -2   /* a CUDA runtime call failed */
 #define PG_ERR_OOM      -3   /* device or pinned-host allocation failed */
-#define PG_ERR_TIMEOUT  -4   /* a bounded device wait ran out (status word set) */
 #define PG_ERR_STATE    -5   /* call order (e.g. pg_align before pg_set_seqs) */
 #define PG_ERR_RANGE    -6   /* a size limit: sequence over 65535 residues, output capacity, product bound */
 #define PG_ERR_NODEV    -7   /* no CUDA device / device id out of range */
@@ -253,21 +252,29 @@ int  pg_align_filtered(pg_ctx *ctx, pg_filter *f, float threshold, const pg_pair
                        uint64_t *kept);
 
 /* Local alignment (--sfa semantics, cfg->mode must be PG_MODE_SW) for callers
- * that may not allocate device memory: code inside a stream capture, plugins
- * whose host framework owns the device allocator, loops that must not touch
- * the allocator between steps.  No reference counterpart: PASTIS itself never
- * runs on a GPU.  Nothing is allocated; the caller passes every input and
- * output as device buffers (sequences as residue codes 0..24 in the order
- * ARNDCQEGHILKMFPSTWYVBZX*J, offsets of nrows+1 / ncols+1 entries, pairs,
- * results), and the kernel's scratch (work counter, status, score table, one
- * DP row per warp) lives in one fixed 32 MiB device array that every GPU
- * loading the library keeps until the process exits.  max_col_len bounds the
- * column sequences (at most 65535); a longer one is rejected with
- * PG_ERR_RANGE.  The first call on a device looks up the array's device
- * address, so make that first call before any stream capture.  Calls share
- * the array: two calls that overlap on the GPU (other streams or threads)
- * race, so serialize them.  Returns after the batch has finished on `stream`
- * (NULL = the legacy default stream); results equal pg_align's bit for bit. */
+ * that may not allocate device memory: plugins running inside a host framework
+ * that owns the device memory pool (its allocator must not be bypassed, and a
+ * cudaMalloc there can fail or stall other work on the device), and step loops
+ * that must not call the allocator between steps.  No reference counterpart:
+ * PASTIS itself never runs on a GPU.  Nothing is allocated; the caller passes
+ * every input and output as device buffers (sequences as residue codes 0..24
+ * in the order ARNDCQEGHILKMFPSTWYVBZX*J, offsets of nrows+1 / ncols+1
+ * entries, pairs, results), and the kernel's scratch (work counter, status,
+ * score table, one DP row per warp) lives in one fixed 32 MiB device array
+ * that every GPU loading the library keeps until the process exits.  The
+ * kernel is the statistics-carrying SW form, about 2.5 times the DP time of
+ * pg_align's default traceback form, which needs an arena this array cannot
+ * hold.  Limits: max_col_len bounds the column sequences (at most 65535; a
+ * longer one gives PG_ERR_RANGE), rows are at most 65535 residues, and one
+ * call takes at most 2^31 - 1 pairs.  Errors: PG_ERR_ARG for a residue code
+ * outside 0..24 (nothing is aligned, d_out is left as it was) or a pair whose
+ * sequence index is out of range (its result is the empty one), PG_ERR_RANGE
+ * for a sequence over the limits (its result is the empty one).  The first
+ * call on a device looks up the array's device address.  Every call clears
+ * the counters and status it uses at its start; calls share the array, so two
+ * calls that overlap on the GPU (other streams or threads) race: serialize
+ * them.  The call synchronizes `stream` (NULL = the legacy default stream)
+ * before it returns; results equal pg_align's bit for bit. */
 int pg_align_sw_noalloc(const pg_config *cfg,
                         const uint8_t *d_row_codes, const uint64_t *d_row_offsets, uint64_t nrows,
                         const uint8_t *d_col_codes, const uint64_t *d_col_offsets, uint64_t ncols,

@@ -16,7 +16,9 @@ extern "C" {
 #endif
 
 /* A caller-supplied aligner for pgh_pw_aln_batch: fills score_aln[0..n) for
- * pairs[0..n) (used to test the driver's pruning and batching without a GPU). */
+ * pairs[0..n) (used to test the driver's pruning and batching without a GPU).
+ * A nonzero return fails the batch: a negative value is returned as the
+ * error code, a positive one as PG_ERR_STATE. */
 typedef int (*pgh_align_cb)(const pg_pair *pairs, uint64_t n, uint64_t bl_roff, uint64_t bl_coff,
                             float *score_aln, void *user);
 
@@ -36,6 +38,42 @@ int pgh_pw_aln_batch(int mode, const pg_config *cfg,
                      uint64_t nnz, uint64_t *rows, uint64_t *cols, void *vals,
                      uint64_t bl_roff, uint64_t bl_coff, uint64_t batch_sz, int ckthr, float mosthr,
                      pgh_align_cb cb, void *cb_user, uint64_t *out_stats, double *out_seconds);
+
+/* Batch-level resume of pgh_pw_aln_batch (the --bsz loop of
+ * src/DistPWRunner.cpp:118-132, batch count l_nnz / bsz + 1 at :85-87; the
+ * reference itself has no resume).  The batches depend only on the nonzero
+ * count after the k-mer prune and on batch_sz, so a run can start at any one:
+ *   start_batch  in: batches before it count as aligned (their score_aln is in vals)
+ *   next_batch   out: first batch not aligned
+ *   last_end     out: end of the pair range of the last aligned batch
+ *   complete     out: 1 when every batch is aligned and the score_aln == 0 prune ran
+ * A run that stops early -- on_batch returned nonzero after a batch, or a batch
+ * failed (the call then returns that batch's error code: a PG_ERR_* of the GPU
+ * library, or the callback aligner's negative return value) -- writes back the
+ * triples as the k-mer prune left them, with score_aln set for every batch
+ * before next_batch, and skips the score_aln prune.  Calling again with those
+ * triples and start_batch = next_batch finishes the stage with the result an
+ * uninterrupted run gives. */
+typedef struct pgh_batch_ctl {
+    uint64_t start_batch;
+    uint64_t next_batch;
+    uint64_t last_end;
+    int32_t  complete;
+    int32_t  reserved;
+} pgh_batch_ctl;
+
+/* Called after each aligned batch; a nonzero return stops the run there. */
+typedef int (*pgh_batch_cb)(uint64_t batch, uint64_t beg, uint64_t end, void *user);
+
+/* pgh_pw_aln_batch with ctl (NULL: run every batch) and on_batch (may be NULL). */
+int pgh_pw_aln_batch_resume(int mode, const pg_config *cfg,
+                            const char *rres, const uint64_t *roffs, uint64_t nr,
+                            const char *cres, const uint64_t *coffs, uint64_t nc,
+                            uint64_t nnz, uint64_t *rows, uint64_t *cols, void *vals,
+                            uint64_t bl_roff, uint64_t bl_coff, uint64_t batch_sz, int ckthr,
+                            float mosthr, pgh_align_cb cb, void *cb_user, uint64_t *out_stats,
+                            double *out_seconds, pgh_batch_ctl *ctl, pgh_batch_cb on_batch,
+                            void *on_batch_user);
 
 /* Write n similarity triples as a Matrix Market coordinate file (what PASTIS's
  * --align-file output holds, src/sim_search.cpp:268-269): header

@@ -13,8 +13,9 @@
 // from a SeqSet (row / column sequences of this rank's block) instead of
 // DistFastaData, and the rank's block of the candidate matrix is a LocalMat
 // (column-major nonzeros, the order dcsc->cp / ir / jc walks them in
-// DistPWRunner.cpp:96-105) instead of SpParMat.  Errors throw
-// std::runtime_error carrying pg_last_error(); there is no silent fallback.
+// DistPWRunner.cpp:96-105) instead of SpParMat.  Errors throw pastis::Error
+// (a std::runtime_error with the PG_ERR_* code and pg_last_error()); there is
+// no silent fallback.
 #pragma once
 
 #include <chrono>
@@ -73,6 +74,12 @@ struct params_t {
     int seed_count = 2;
     int ckthr = 0;
     float mosthr = -1.0f;
+};
+
+// an error of the GPU library (or of an aligner's own call) with its code
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &what) : std::runtime_error(what), code(c) {}
 };
 
 // sequences of one side of the block: residues concatenated, offsets[n+1]
@@ -184,8 +191,8 @@ private:
     static void check(int rc)
     {
         if (rc != PG_OK)
-            throw std::runtime_error(std::string("pastis_gb300: ") + pg_strerror(rc) + ": " +
-                                     pg_last_error());
+            throw Error(rc, std::string("pastis_gb300: ") + pg_strerror(rc) + ": " +
+                                pg_last_error());
     }
     static std::vector<uint32_t> lengths(const SeqSet &s)
     {
@@ -216,7 +223,7 @@ private:
             const auto &tu = t[beg + i];
             const uint64_t r = std::get<0>(tu), c = std::get<1>(tu);
             if (r > 0xffffffffull || c > 0xffffffffull)
-                throw std::runtime_error("pastis_gb300: local index above 2^32");
+                throw Error(PG_ERR_ARG, "pastis_gb300: local index above 2^32");
             pg_pair &p = pairs_[i];
             p.row = (uint32_t)r; p.col = (uint32_t)c;
             p.count = std::get<2>(tu)->count;
@@ -261,12 +268,34 @@ struct BatchStats {
     uint64_t nnz_in = 0, nnz_kmer_thr = 0, nnz_aln = 0, batches = 0;
 };
 
+// Batch-level resume around the --bsz loop (src/DistPWRunner.cpp:118-132; the
+// batch count l_nnz / bsz + 1 at :85-87).  The batch boundaries depend only on
+// the pruned nonzero count and bsz, so a run can start at any batch:
+//   start_batch  batches before it count as done (their score_aln is already in C)
+//   on_batch     called after each aligned batch with its index and pair range;
+//                returning false stops the run there (a job stopped between batches)
+//   next_batch   out: the first batch not aligned (batch_cnt when all are)
+//   last_end     out: end of the last aligned batch's pair range
+//   complete     out: every batch aligned and the score_aln == 0 prune done
+// A run that stops early, by on_batch or by an aligner error (which is then
+// rethrown), leaves C as the k-mer prune left it, with score_aln written for
+// every batch before next_batch, and does not run the score_aln prune.  Calling
+// pw_aln_batch again on that C with start_batch = next_batch finishes the
+// stage; the k-mer prune is idempotent, so the batches are the same.
+struct BatchControl {
+    uint64_t start_batch = 0;
+    std::function<bool(uint64_t batch, uint64_t beg, uint64_t end)> on_batch;
+    uint64_t next_batch = 0, last_end = 0;
+    bool complete = false;
+};
+
 // src/DistPWRunner.cpp:25-165 on one rank's block: k-mer threshold prune,
 // tuples, --bsz batches (batch_cnt = l_nnz / bsz + 1, so the trailing batch may
 // be empty), then drop entries whose score_aln is 0.
 template <typename NT>
 BatchStats pw_aln_batch(LocalMat<NT> &C, PWAlign &pwa, const params_t &params,
-                        uint64_t bl_roffset = 0, uint64_t bl_coffset = 0)
+                        uint64_t bl_roffset = 0, uint64_t bl_coffset = 0,
+                        BatchControl *ctl = nullptr)
 {
     BatchStats st;
     st.nnz_in = C.nnz();
@@ -276,27 +305,52 @@ BatchStats pw_aln_batch(LocalMat<NT> &C, PWAlign &pwa, const params_t &params,
     st.nnz_kmer_thr = C.nnz();
     pwa.tp.start("align");
     const uint64_t l_nnz = C.nnz();
+    bool stopped = false;
     if (l_nnz != 0) {
         const uint64_t bsz = params.aln_batch_sz ? params.aln_batch_sz : 1;
         const uint64_t batch_cnt = l_nnz / bsz + 1;
+        const uint64_t b0 = ctl ? ctl->start_batch : 0;
+        if (ctl) { ctl->next_batch = b0 < batch_cnt ? b0 : batch_cnt; ctl->last_end = 0; }
         pwa.tp.start("align|form-tuples");
         std::vector<std::tuple<uint64_t, uint64_t, NT *>> tuples(l_nnz);
         for (uint64_t k = 0; k < l_nnz; ++k) tuples[k] = std::make_tuple(C.row[k], C.col[k], &C.val[k]);
         pwa.tp.stop("align|form-tuples");
         pwa.tp.start("align|batch");
-        for (uint64_t b = 0; b < batch_cnt; ++b) {
+        for (uint64_t b = b0; b < batch_cnt; ++b) {
             const uint64_t beg = b * bsz;
             const uint64_t end = (b + 1) * bsz > l_nnz ? l_nnz : (b + 1) * bsz;
-            pwa.aln_batch(tuples.data(), beg, end, bl_roffset, bl_coffset, params);
+            try {
+                pwa.aln_batch(tuples.data(), beg, end, bl_roffset, bl_coffset, params);
+            } catch (...) {
+                pwa.tp.stop("align|batch");
+                pwa.tp.stop("align");
+                throw;
+            }
             ++st.batches;
+            if (ctl) {
+                ctl->next_batch = b + 1;
+                ctl->last_end = end;
+                if (ctl->on_batch && !ctl->on_batch(b, beg, end) && b + 1 < batch_cnt) {
+                    stopped = true;
+                    break;
+                }
+            }
         }
         pwa.tp.stop("align|batch");
+    } else if (ctl) {
+        ctl->next_batch = 0;
+        ctl->last_end = 0;
     }
     pwa.tp.stop("align");
+    if (stopped) {
+        st.nnz_aln = C.nnz();
+        return st;
+    }
     pwa.tp.start("prune");
     C.prune([](const NT &v) { return v.score_aln == 0.0f; });
     pwa.tp.stop("prune");
     st.nnz_aln = C.nnz();
+    if (ctl) ctl->complete = true;
     return st;
 }
 

@@ -96,6 +96,22 @@ def make_params(gap_first=-11, gap_ext=-2, xdrop_gap=None, xdrop=49, seed_len=6,
     return p
 
 
+def pastis_params(as_called=True, **over):
+    """PASTIS's alignment defaults (src/main.cpp:97-116, :158-166): gap open
+    -11, gap extend -2, x = 49, k = 6, two seeds, coverage 0.7, ANI 30.
+
+    as_called: the gaps reach SeqAn's Score(gapExtend, gapOpen) constructor in
+    the order PASTIS passes them (src/align/SeqanXdropAligner.hpp:38-43), so
+    the first gap position scores -2, further positions -11 and the X-drop
+    extension's linear gap is -11.  Otherwise the nominal reading: first -11,
+    further -2, X-drop gap -2."""
+    first, ext = (-2, -11) if as_called else (-11, -2)
+    kw = dict(gap_first=first, gap_ext=ext, xdrop_gap=ext, xdrop=49, seed_len=6, seed_count=2,
+              tie=0, flags=0, cov_thr=0.7, ani_thr=30)
+    kw.update(over)
+    return make_params(**kw)
+
+
 def _u8(a):
     return np.ascontiguousarray(a, dtype=np.uint8)
 

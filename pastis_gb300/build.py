@@ -58,11 +58,15 @@ def _stale(out, deps):
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
-def build(force=False, verbose=False):
+def build(force=False, verbose=False, only=None):
+    """Build every library, or only the outputs named in ``only`` (e.g.
+    {"libpastis_synth.so"}: the generator alone, no CUDA compile)."""
     os.makedirs(BUILD, exist_ok=True)
     for jobs in _steps():
         procs = []
         for name, cmd, deps in jobs:
+            if only is not None and name not in only:
+                continue
             out = os.path.join(BUILD, name)
             if not force and not _stale(out, deps):
                 continue

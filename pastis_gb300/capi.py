@@ -13,30 +13,15 @@ from . import build as _build
 BUILD = _build.BUILD
 
 PG_OK = 0
-PG_ERR_ARG, PG_ERR_CUDA, PG_ERR_OOM, PG_ERR_TIMEOUT = -1, -2, -3, -4
+PG_ERR_ARG, PG_ERR_CUDA, PG_ERR_OOM = -1, -2, -3
 PG_ERR_STATE, PG_ERR_RANGE, PG_ERR_NODEV = -5, -6, -7
 MODE_SW, MODE_XDROP = 0, 1
 GAPS_AS_CALLED, GAPS_NOMINAL = 0, 1
 TIE_H_E_BEFORE_F, TIE_GAP_OPEN_FIRST = 1, 2
 F_SKIP_SPURIOUS_SEED = 1
 RF_EMPTY, RF_BAD_SEED, RF_PASSED, RF_FILTERED = 1, 2, 4, 8
-NRES = 25
-LETTERS = "ARNDCQEGHILKMFPSTWYVBZX*J"
-
-PAIR_DTYPE = np.dtype([("row", "<u4"), ("col", "<u4"), ("rs0", "<u2"), ("cs0", "<u2"),
-                       ("rs1", "<u2"), ("cs1", "<u2"), ("count", "<u2"), ("score", "<i2")])
-RESULT_DTYPE = np.dtype([("score", "<i4"), ("aln_len", "<u4"), ("matches", "<u4"),
-                         ("gap_opens", "<u4"), ("beg_h", "<u2"), ("end_h", "<u2"),
-                         ("beg_v", "<u2"), ("end_v", "<u2"), ("identity", "<f4"),
-                         ("score_aln", "<f4"), ("seed_used", "u1"), ("flags", "u1"),
-                         ("pad", "<u2"), ("cells", "<u4")])
-# inc/Types.hpp CommonKmerLoc (16 B) and CommonKmerLight (8 B)
-KMERLOC_DTYPE = np.dtype([("count", "<u2"), ("score", "<i2"), ("score_aln", "<f4"),
-                          ("first_r", "<u2"), ("first_c", "<u2"),
-                          ("second_r", "<u2"), ("second_c", "<u2")])
-KMERLIGHT_DTYPE = np.dtype([("count", "<u2"), ("score", "<i2"), ("score_aln", "<f4")])
-assert PAIR_DTYPE.itemsize == 20 and RESULT_DTYPE.itemsize == 40
-assert KMERLOC_DTYPE.itemsize == 16 and KMERLIGHT_DTYPE.itemsize == 8
+from .records import (KMERLIGHT_DTYPE, KMERLOC_DTYPE, LETTERS, NRES,  # noqa: F401
+                      PAIR_DTYPE, RESULT_DTYPE, decode)
 
 # every entry point declared in include/*.h (checked by the CPU tests)
 EXPORTS = {
@@ -54,7 +39,8 @@ EXPORTS = {
                            "pg_synth_nres", "pg_synth_npairs", "pg_synth_seq", "pg_synth_offs",
                            "pg_synth_family", "pg_synth_pairs", "pg_synth_homolog",
                            "pg_synth_spurious"],
-    "libpastis_host.so": ["pgh_pw_aln_batch", "pgh_last_error", "pgh_write_mm"],
+    "libpastis_host.so": ["pgh_pw_aln_batch", "pgh_pw_aln_batch_resume", "pgh_last_error",
+                          "pgh_write_mm"],
 }
 
 
@@ -193,17 +179,8 @@ def _declare(name, lib):
         lib.pg_last_error.restype = ctypes.c_char_p
         lib.pg_version.restype = ctypes.c_char_p
     elif name == "libpastis_synth.so":
-        lib.pg_synth_generate.argtypes = [vp]
-        lib.pg_synth_generate.restype = vp
-        for f in ("pg_synth_nseqs", "pg_synth_nres", "pg_synth_npairs"):
-            getattr(lib, f).argtypes = [vp]
-            getattr(lib, f).restype = u64
-        for f in ("pg_synth_seq", "pg_synth_offs", "pg_synth_family", "pg_synth_pairs",
-                  "pg_synth_homolog", "pg_synth_spurious"):
-            getattr(lib, f).argtypes = [vp]
-            getattr(lib, f).restype = vp
-        lib.pg_synth_free.argtypes = [vp]
-        lib.pg_synth_free.restype = None
+        from .synth import declare
+        declare(lib)
     elif name == "libpastis_host.so":
         lib.pgh_last_error.restype = ctypes.c_char_p
         lib.pgh_write_mm.argtypes = [ctypes.c_char_p, u64, u64, vp, vp, vp, u64]
@@ -243,11 +220,6 @@ def dpx_peak(device=0):
     v = ctypes.c_double()
     _check(load().pg_dpx_peak(device, ctypes.byref(v)))
     return v.value
-
-
-def decode(codes):
-    lut = np.frombuffer(LETTERS.encode(), dtype=np.uint8)
-    return lut[np.asarray(codes, dtype=np.uint8)]
 
 
 class Context:
@@ -377,16 +349,42 @@ class Context:
 
 ALIGN_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
                             ctypes.c_uint64, ctypes.POINTER(ctypes.c_float), ctypes.c_void_p)
+BATCH_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                            ctypes.c_void_p)
+
+
+class BatchCtl(ctypes.Structure):
+    """pgh_batch_ctl: batch-level resume of pw_aln_batch."""
+    _fields_ = [("start_batch", ctypes.c_uint64), ("next_batch", ctypes.c_uint64),
+                ("last_end", ctypes.c_uint64), ("complete", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class BatchError(RuntimeError):
+    """A batch of pw_aln_batch failed.  ``code`` is its PG_ERR_* code and
+    ``partial`` the (rows, cols, vals, stats) the driver wrote back: the
+    triples after the k-mer prune with score_aln set for every batch before
+    stats["next_batch"], ready to resume from there."""
+
+    def __init__(self, code, detail, partial):
+        super().__init__("pw_aln_batch failed (%d): %s" % (code, detail))
+        self.code = code
+        self.partial = partial
 
 
 def pw_aln_batch(mode, rows, cols, vals, row_res, row_offs, col_res=None, col_offs=None,
                  bl_roff=0, bl_coff=0, batch_sz=10 ** 10, ckthr=0, mosthr=-1.0, cfg=None,
-                 callback=None):
+                 callback=None, start_batch=0, on_batch=None):
     """Run the C++ pw_aln_batch driver (src/DistPWRunner.cpp:25-165) on one block.
 
     vals is a KMERLOC_DTYPE (X-drop) or KMERLIGHT_DTYPE (SW) array.  With
     ``callback(pairs, bl_roff, bl_coff) -> score_aln array`` the driver uses it
-    as the aligner instead of the GPU.  Returns (rows, cols, vals, stats)."""
+    as the aligner instead of the GPU (raising in it fails the batch with
+    PG_ERR_STATE; returning an int < 0 fails it with that code).  Batch-level
+    resume: ``start_batch`` skips the batches before it, and
+    ``on_batch(batch, beg, end) -> bool`` is called after each batch, False
+    stopping the run there.  Returns (rows, cols, vals, stats); stats holds
+    next_batch, last_end and complete.  A failed batch raises BatchError."""
     lib = load("libpastis_host.so")
     rows = np.array(rows, dtype=np.uint64)
     cols = np.array(cols, dtype=np.uint64)
@@ -407,26 +405,41 @@ def pw_aln_batch(mode, rows, cols, vals, row_res, row_offs, col_res=None, col_of
             try:
                 arr = np.ctypeslib.as_array((ctypes.c_char * (n * PAIR_DTYPE.itemsize))
                                             .from_address(pp)).view(PAIR_DTYPE).copy()
-                s = np.ascontiguousarray(callback(arr, ro, co), dtype=np.float32)
+                r = callback(arr, ro, co)
+                if isinstance(r, int):
+                    return r if r < 0 else 1
+                s = np.ascontiguousarray(r, dtype=np.float32)
                 ctypes.memmove(out, s.ctypes.data, 4 * n)
                 return 0
             except Exception:
                 return 1
         cb = ALIGN_CB(_cb)
+    bcb = None
+    if on_batch is not None:
+        def _bcb(b, beg, end, user):
+            try:
+                return 0 if on_batch(int(b), int(beg), int(end)) else 1
+            except Exception:
+                return 1
+        bcb = BATCH_CB(_bcb)
+    ctl = BatchCtl()
+    ctl.start_batch = start_batch
     c = cfg if cfg is not None else config(mode)
     vp, u64 = ctypes.c_void_p, ctypes.c_uint64
-    rc = lib.pgh_pw_aln_batch(ctypes.c_int(mode), ctypes.byref(c), vp(rres.ctypes.data),
-                              vp(roffs.ctypes.data), u64(len(roffs) - 1), vp(cres_p),
-                              vp(coffs_p), u64(nc), u64(len(vals)), vp(rows.ctypes.data),
-                              vp(cols.ctypes.data), vp(vals.ctypes.data), u64(bl_roff),
-                              u64(bl_coff), u64(batch_sz), ctypes.c_int(ckthr),
-                              ctypes.c_float(mosthr), cb, None, vp(stats.ctypes.data),
-                              vp(secs.ctypes.data))
-    if rc != PG_OK:
-        raise RuntimeError("pw_aln_batch failed (%d): %s" % (rc, lib.pgh_last_error().decode()))
+    rc = lib.pgh_pw_aln_batch_resume(
+        ctypes.c_int(mode), ctypes.byref(c), vp(rres.ctypes.data), vp(roffs.ctypes.data),
+        u64(len(roffs) - 1), vp(cres_p), vp(coffs_p), u64(nc), u64(len(vals)),
+        vp(rows.ctypes.data), vp(cols.ctypes.data), vp(vals.ctypes.data), u64(bl_roff),
+        u64(bl_coff), u64(batch_sz), ctypes.c_int(ckthr), ctypes.c_float(mosthr), cb, None,
+        vp(stats.ctypes.data), vp(secs.ctypes.data), ctypes.byref(ctl), bcb, None)
     k = int(stats[2])
-    return rows[:k], cols[:k], vals[:k], {
-        "nnz_in": int(stats[0]), "nnz_kmer_thr": int(stats[1]), "nnz_aln": int(stats[2]),
-        "batches": int(stats[3]), "empty_batches": int(stats[4]),
-        "seconds": {"align|pre": secs[0], "align|gpu": secs[1], "align|post": secs[2],
-                    "align": secs[3]}}
+    st = {"nnz_in": int(stats[0]), "nnz_kmer_thr": int(stats[1]), "nnz_aln": int(stats[2]),
+          "batches": int(stats[3]), "empty_batches": int(stats[4]),
+          "next_batch": int(ctl.next_batch), "last_end": int(ctl.last_end),
+          "complete": bool(ctl.complete),
+          "seconds": {"align|pre": secs[0], "align|gpu": secs[1], "align|post": secs[2],
+                      "align": secs[3]}}
+    if rc != PG_OK:
+        raise BatchError(rc, lib.pgh_last_error().decode(errors="replace"),
+                         (rows[:k], cols[:k], vals[:k], st))
+    return rows[:k], cols[:k], vals[:k], st

@@ -3,7 +3,8 @@
 //
 // pgh_pw_aln_batch runs pw_aln_batch (src/DistPWRunner.cpp:25-165) on one
 // rank's block with either the GPU aligner or a caller-supplied aligner
-// callback (used to test the driver's pruning and batching without a GPU).
+// callback (used to test the driver's pruning and batching without a GPU);
+// pgh_pw_aln_batch_resume adds batch-level resume (pastis::BatchControl).
 #include <cstdio>
 #include <cstring>
 #include <exception>
@@ -58,8 +59,9 @@ private:
             q.score = std::get<2>(t[i])->score;
             seeds(q, std::get<2>(t[i]));
         }
-        if (cb_(p.data(), end - beg, ro, co, s.data(), user_) != 0)
-            throw std::runtime_error("aligner callback failed");
+        const int rc = cb_(p.data(), end - beg, ro, co, s.data(), user_);
+        if (rc != 0)
+            throw pastis::Error(rc < 0 ? rc : PG_ERR_STATE, "aligner callback failed");
         for (uint64_t i = beg; i < end; ++i) std::get<2>(t[i])->score_aln = s[i - beg];
     }
 };
@@ -68,7 +70,8 @@ template <typename NT>
 int drive(int mode, const pg_config *cfg, const char *rres, const uint64_t *roffs, uint64_t nr,
           const char *cres, const uint64_t *coffs, uint64_t nc, uint64_t nnz, uint64_t *rows,
           uint64_t *cols, NT *vals, uint64_t bl_roff, uint64_t bl_coff, uint64_t batch_sz, int ckthr,
-          float mosthr, pgh_align_cb cb, void *cb_user, uint64_t *out_stats, double *out_seconds)
+          float mosthr, pgh_align_cb cb, void *cb_user, uint64_t *out_stats, double *out_seconds,
+          pgh_batch_ctl *ctl, pgh_batch_cb on_batch, void *on_batch_user)
 {
     pastis::params_t params;
     params.aln_batch_sz = batch_sz;
@@ -102,8 +105,34 @@ int drive(int mode, const pg_config *cfg, const char *rres, const uint64_t *roff
             pwa->construct_seqs_bl(R);
         }
     }
-    st = pastis::pw_aln_batch(C, *pwa, params, bl_roff, bl_coff);
+    pastis::BatchControl bc;
+    if (ctl) {
+        bc.start_batch = ctl->start_batch;
+        if (on_batch)
+            bc.on_batch = [on_batch, on_batch_user](uint64_t b, uint64_t beg, uint64_t end) {
+                return on_batch(b, beg, end, on_batch_user) == 0;
+            };
+    }
+    // a failed batch: what the earlier batches wrote stays in C, which goes
+    // back to the caller with the error code
+    int rc = PG_OK;
+    st.nnz_in = nnz;
+    try {
+        st = pastis::pw_aln_batch(C, *pwa, params, bl_roff, bl_coff, ctl ? &bc : nullptr);
+    } catch (const pastis::Error &e) {
+        g_host_err = e.what();
+        rc = e.code;
+    }
+    if (rc != PG_OK) {
+        // the k-mer prune ran before the batch loop; nothing after it did
+        st.nnz_kmer_thr = st.nnz_aln = C.nnz();
+    }
     for (uint64_t i = 0; i < C.nnz(); ++i) { rows[i] = C.row[i]; cols[i] = C.col[i]; vals[i] = C.val[i]; }
+    if (ctl) {
+        ctl->next_batch = bc.next_batch;
+        ctl->last_end = bc.last_end;
+        ctl->complete = (rc == PG_OK && bc.complete) ? 1 : 0;
+    }
     if (out_stats) {
         out_stats[0] = st.nnz_in; out_stats[1] = st.nnz_kmer_thr; out_stats[2] = st.nnz_aln;
         out_stats[3] = st.batches;
@@ -116,10 +145,43 @@ int drive(int mode, const pg_config *cfg, const char *rres, const uint64_t *roff
         out_seconds[2] = pwa->tp.seconds["align|post"];
         out_seconds[3] = pwa->tp.seconds["align"];
     }
-    return PG_OK;
+    return rc;
 }
 
 }  // namespace
+
+extern "C" int pgh_pw_aln_batch_resume(int mode, const pg_config *cfg,
+                                       const char *rres, const uint64_t *roffs, uint64_t nr,
+                                       const char *cres, const uint64_t *coffs, uint64_t nc,
+                                       uint64_t nnz, uint64_t *rows, uint64_t *cols, void *vals,
+                                       uint64_t bl_roff, uint64_t bl_coff, uint64_t batch_sz,
+                                       int ckthr, float mosthr, pgh_align_cb cb, void *cb_user,
+                                       uint64_t *out_stats, double *out_seconds,
+                                       pgh_batch_ctl *ctl, pgh_batch_cb on_batch,
+                                       void *on_batch_user)
+{
+    if (nnz && (!rows || !cols || !vals)) {
+        g_host_err = "pgh_pw_aln_batch: null triple array";
+        return PG_ERR_ARG;
+    }
+    try {
+        if (mode == PG_MODE_XDROP)
+            return drive(mode, cfg, rres, roffs, nr, cres, coffs, nc, nnz, rows, cols,
+                         (pastis::CommonKmerLoc *)vals, bl_roff, bl_coff, batch_sz, ckthr, mosthr,
+                         cb, cb_user, out_stats, out_seconds, ctl, on_batch, on_batch_user);
+        if (mode == PG_MODE_SW)
+            return drive(mode, cfg, rres, roffs, nr, cres, coffs, nc, nnz, rows, cols,
+                         (pastis::CommonKmerLight *)vals, bl_roff, bl_coff, batch_sz, ckthr, mosthr,
+                         cb, cb_user, out_stats, out_seconds, ctl, on_batch, on_batch_user);
+        return PG_ERR_ARG;
+    } catch (const pastis::Error &e) {
+        g_host_err = e.what();
+        return e.code;
+    } catch (const std::exception &e) {
+        g_host_err = e.what();
+        return PG_ERR_STATE;
+    }
+}
 
 extern "C" int pgh_pw_aln_batch(int mode, const pg_config *cfg,
                                 const char *rres, const uint64_t *roffs, uint64_t nr,
@@ -129,20 +191,9 @@ extern "C" int pgh_pw_aln_batch(int mode, const pg_config *cfg,
                                 float mosthr, pgh_align_cb cb, void *cb_user, uint64_t *out_stats,
                                 double *out_seconds)
 {
-    try {
-        if (mode == PG_MODE_XDROP)
-            return drive(mode, cfg, rres, roffs, nr, cres, coffs, nc, nnz, rows, cols,
-                         (pastis::CommonKmerLoc *)vals, bl_roff, bl_coff, batch_sz, ckthr, mosthr,
-                         cb, cb_user, out_stats, out_seconds);
-        if (mode == PG_MODE_SW)
-            return drive(mode, cfg, rres, roffs, nr, cres, coffs, nc, nnz, rows, cols,
-                         (pastis::CommonKmerLight *)vals, bl_roff, bl_coff, batch_sz, ckthr, mosthr,
-                         cb, cb_user, out_stats, out_seconds);
-        return PG_ERR_ARG;
-    } catch (const std::exception &e) {
-        g_host_err = e.what();
-        return PG_ERR_STATE;
-    }
+    return pgh_pw_aln_batch_resume(mode, cfg, rres, roffs, nr, cres, coffs, nc, nnz, rows, cols,
+                                   vals, bl_roff, bl_coff, batch_sz, ckthr, mosthr, cb, cb_user,
+                                   out_stats, out_seconds, nullptr, nullptr, nullptr);
 }
 
 extern "C" int pgh_write_mm(const char *path, uint64_t nrows, uint64_t ncols, const uint64_t *rows,

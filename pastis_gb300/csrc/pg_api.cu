@@ -205,7 +205,6 @@ const char *pg_strerror(int code)
     case PG_ERR_ARG: return "invalid argument";
     case PG_ERR_CUDA: return "CUDA error";
     case PG_ERR_OOM: return "out of memory";
-    case PG_ERR_TIMEOUT: return "device wait timed out";
     case PG_ERR_STATE: return "invalid call order";
     case PG_ERR_RANGE: return "sequence longer than 65535 residues";
     case PG_ERR_NODEV: return "no usable CUDA device";
@@ -929,19 +928,29 @@ int pg_kernel_ms(pg_ctx *c, float out[2])
 
 // ------------------------------------------------- no-allocation SW entry point
 //
-// For callers that may not allocate device memory at all: code running inside
-// a stream capture or a driver that owns the whole device pool, plugins
-// embedded in a host framework whose allocator must not be bypassed, or
-// real-time loops that must not touch the allocator between steps.  Instead
-// of a context's cudaMalloc'd scratch, the local-alignment kernel below keeps
-// its work counter, status word, score table and per-warp DP rows in one
+// For callers that may not allocate device memory at all: plugins embedded in
+// a host framework that owns the device memory pool (its allocator must not be
+// bypassed, and a cudaMalloc there can fail or serialise the whole device), and
+// step loops that must not call the allocator between steps.  Instead of a
+// context's cudaMalloc'd scratch, the local-alignment kernel below keeps its
+// work counter, status word, score table and per-warp DP rows in one
 // file-scope device array of fixed size.  Every GPU that loads the library
-// holds that array until the process exits.
+// holds that array until the process exits.  The kernel is the
+// statistics-carrying SW form (k_sw's recurrence), which needs no direction
+// arena: about 2.5 times the DP time of pg_align's default traceback form.
 namespace {
 
 constexpr size_t kNoAllocBytes = (size_t)32 << 20;   // PG_NOALLOC_SCRATCH_BYTES
 constexpr size_t kNoAllocHeader = 4096;              // counters, status, score table
 constexpr int kMaxDevices = 64;
+// byte offsets inside the array's header
+constexpr size_t kNaCounters = 0;     // [0, 16): the work-queue counters
+constexpr size_t kNaStatus = 16;      // [16, 20): status word (ST_* bits)
+constexpr size_t kNaExec = 24;        // [24, 40): executed cells (X-drop, DP)
+constexpr size_t kNaCleared = 64;     // [0, 64) is zeroed by every call
+constexpr size_t kNaTable = 64;       // [64, 64 + 625): the score table
+// the work queue's counter is 32-bit: it must not wrap while warps still pop
+constexpr uint64_t kNoAllocMaxPairs = (1ull << 31) - 1;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -950,11 +959,29 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 std::mutex g_noalloc_mu;
 void *g_noalloc_ptr[kMaxDevices] = {};
 
+// residue codes the caller passed: any code outside 0..24 sets ST_BAD_CODE
+// (the DP indexes its score tables by code)
+__global__ void k_noalloc_codes(const uint8_t *__restrict__ rseq, const uint64_t *__restrict__ roffs,
+                                uint64_t nr, const uint8_t *__restrict__ cseq,
+                                const uint64_t *__restrict__ coffs, uint64_t nc, int *status)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool bad = false;
+    const uint64_t rb = roffs[0], re = roffs[nr];
+    for (uint64_t i = rb + t0; i < re; i += stride) bad |= rseq[i] >= PG_NRES;
+    const uint64_t cb = coffs[0], ce = coffs[nc];
+    for (uint64_t i = cb + t0; i < ce; i += stride) bad |= cseq[i] >= PG_NRES;
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(status, pg::ST_BAD_CODE);
+}
+
 // k_sw with the per-pair column length checked against the rows it was given
 template <int TIE>
 __global__ void __launch_bounds__(pg::WARPS * 32) k_sw_noalloc(const pg::KParams kp, int max_cols)
 {
     __shared__ int ssm[32 * 32];
+    // bad residue codes: align nothing (the call reports PG_ERR_ARG)
+    if (*(volatile int *)kp.status & pg::ST_BAD_CODE) return;
     pg::load_sm(ssm, kp.sm);
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -973,8 +1000,9 @@ __global__ void __launch_bounds__(pg::WARPS * 32) k_sw_noalloc(const pg::KParams
             if (lane == 0) { atomicOr(kp.status, pg::ST_BAD_INDEX); kp.out[p] = o; }
             continue;
         }
-        if (n > max_cols || m > 65535) {
-            if (lane == 0) { atomicOr(kp.status, 2); kp.out[p] = o; }
+        // decreasing offsets give negative lengths
+        if (m < 0 || n < 0 || n > max_cols || m > 65535) {
+            if (lane == 0) { atomicOr(kp.status, pg::ST_TOO_LONG); kp.out[p] = o; }
             continue;
         }
         exec += (unsigned long long)m * (unsigned long long)n;
@@ -1027,7 +1055,8 @@ extern "C" int pg_align_sw_noalloc(const pg_config *cfg,
     if (n == 0) return PG_OK;
     if (!d_row_codes || !d_row_offsets || !d_col_codes || !d_col_offsets || !d_pairs || !d_out)
         return fail(PG_ERR_ARG, "pg_align_sw_noalloc: null buffer");
-    if (n > 0xffffffffull) return fail(PG_ERR_ARG, "pg_align_sw_noalloc: more than 2^32-1 pairs");
+    if (n > kNoAllocMaxPairs)
+        return fail(PG_ERR_ARG, "pg_align_sw_noalloc: more than 2^31-1 pairs in one call");
     if (max_col_len > 65535)
         return fail(PG_ERR_RANGE, "pg_align_sw_noalloc: max_col_len %u above 65535", max_col_len);
     const size_t per_warp = (((size_t)max_col_len + 1) * sizeof(pg::Edge<pg::L2>) + 255) & ~(size_t)255;
@@ -1059,27 +1088,27 @@ extern "C" int pg_align_sw_noalloc(const pg_config *cfg,
         base = (unsigned char *)g_noalloc_ptr[cfg->device];
     }
     cudaStream_t st = (cudaStream_t)stream;
-    // header: [0,16) counters, [16,20) status, [24,32) executed cells,
-    // [64, 64+625) score table; DP rows from kNoAllocHeader on
+    // the header (counters, status, executed cells) starts at zero on every
+    // call; the array keeps whatever the previous call left
     int8_t table[PG_NRES * PG_NRES];
     if (cfg->score_matrix) std::memcpy(table, cfg->score_matrix, sizeof table);
     else blosum62(table);
-    CU(cudaMemsetAsync(base, 0, 64, st));
-    CU(cudaMemcpyAsync(base + 64, table, sizeof table, cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(base, 0, kNaCleared, st));
+    CU(cudaMemcpyAsync(base + kNaTable, table, sizeof table, cudaMemcpyHostToDevice, st));
     pg::KParams kp;
     std::memset(&kp, 0, sizeof kp);
     kp.pairs = d_pairs; kp.n = n; kp.roff = bl_roffset; kp.coff = bl_coffset;
     kp.rseq = d_row_codes; kp.roffs = d_row_offsets; kp.nr = nrows;
     kp.cseq = d_col_codes; kp.coffs = d_col_offsets; kp.nc = ncols;
-    kp.out = d_out; kp.sm = (const int8_t *)(base + 64);
+    kp.out = d_out; kp.sm = (const int8_t *)(base + kNaTable);
     if (cfg->gap_semantics == PG_GAPS_AS_CALLED) { kp.go = cfg->gap_ext; kp.ge = cfg->gap_open; }
     else { kp.go = cfg->gap_open; kp.ge = cfg->gap_ext; }
     kp.xg = kp.ge; kp.xdrop = cfg->xdrop; kp.seed_len = cfg->seed_len;
     kp.seed_count = cfg->seed_count; kp.flags = cfg->flags;
     kp.ani_thr = cfg->ani_thr; kp.cov_thr = cfg->cov_thr;
-    kp.counter = (unsigned int *)base;
-    kp.status = (int *)(base + 16);
-    kp.exec_cells = (unsigned long long *)(base + 24);
+    kp.counter = (unsigned int *)(base + kNaCounters);
+    kp.status = (int *)(base + kNaStatus);
+    kp.exec_cells = (unsigned long long *)(base + kNaExec);
     kp.bnd = base + kNoAllocHeader;
     kp.bnd_bytes = per_warp;
     int nsm = 0, per_sm = 0;
@@ -1090,6 +1119,8 @@ extern "C" int pg_align_sw_noalloc(const pg_config *cfg,
     grid = std::min<uint64_t>(grid, (n + pg::WARPS - 1) / pg::WARPS);
     const dim3 blk(pg::WARPS * 32);
     const int dyn = pg::DP_DYN_SMEM;
+    k_noalloc_codes<<<(unsigned)nsm * 4u, 256, 0, st>>>(d_row_codes, d_row_offsets, nrows, d_col_codes,
+                                                       d_col_offsets, ncols, kp.status);
     switch (cfg->tie) {
     case 0: k_sw_noalloc<0><<<(unsigned)grid, blk, dyn, st>>>(kp, (int)max_col_len); break;
     case 1: k_sw_noalloc<1><<<(unsigned)grid, blk, dyn, st>>>(kp, (int)max_col_len); break;
@@ -1098,11 +1129,13 @@ extern "C" int pg_align_sw_noalloc(const pg_config *cfg,
     }
     CU(cudaGetLastError());
     int status = 0;
-    CU(cudaMemcpyAsync(&status, base + 16, sizeof status, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&status, base + kNaStatus, sizeof status, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
+    if (status & pg::ST_BAD_CODE)
+        return fail(PG_ERR_ARG, "pg_align_sw_noalloc: a residue code outside 0..24 (nothing aligned)");
     if (status & pg::ST_BAD_INDEX)
         return fail(PG_ERR_ARG, "pg_align_sw_noalloc: a pair refers to a sequence index out of range");
-    if (status & 2)
+    if (status & pg::ST_TOO_LONG)
         return fail(PG_ERR_RANGE, "pg_align_sw_noalloc: a column sequence is longer than max_col_len %u "
                     "or a row sequence longer than 65535", max_col_len);
     return PG_OK;

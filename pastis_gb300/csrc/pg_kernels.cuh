@@ -43,7 +43,9 @@ constexpr int XW = 16;            // per-thread ring slots in k_xdf
 
 // status word bits (read back by the host after a batch)
 constexpr int ST_BAD_INDEX = 1;
+constexpr int ST_TOO_LONG = 2;    // a sequence beyond a kernel's length bound
 constexpr int ST_BAD_SCHED = 4;   // bucket order inconsistent (never expected)
+constexpr int ST_BAD_CODE = 8;    // a residue code outside 0..24
 
 // extension of one (pair, seed)
 constexpr uint32_t XF_NONE = 1;    // seed not tried (seed_count / spurious switch)

@@ -10,6 +10,7 @@ Workload presets follow the benchmark definitions of this stage:
              6-mers, X-drop x = 49
   uneven10m  10M pairs, lengths 80 % lognormal (median 300) + 20 % uniform
              1000-5000, min 20
+  uneven10m_sw  the same batch, aligned by local Smith-Waterman
   filter5m   5M pairs of the sw100k generator at a 30 % homolog rate (the
              learned filter's training and evaluation set)
   manytomany 1M proteins in families of 2-50 at 30-90 % identity; its
@@ -20,7 +21,36 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import capi
+from . import records
+
+
+def declare(lib):
+    """Argument and return types of libpastis_synth.so's entry points."""
+    vp, u64 = ctypes.c_void_p, ctypes.c_uint64
+    lib.pg_synth_generate.argtypes = [vp]
+    lib.pg_synth_generate.restype = vp
+    for f in ("pg_synth_nseqs", "pg_synth_nres", "pg_synth_npairs"):
+        getattr(lib, f).argtypes = [vp]
+        getattr(lib, f).restype = u64
+    for f in ("pg_synth_seq", "pg_synth_offs", "pg_synth_family", "pg_synth_pairs",
+              "pg_synth_homolog", "pg_synth_spurious"):
+        getattr(lib, f).argtypes = [vp]
+        getattr(lib, f).restype = vp
+    lib.pg_synth_free.argtypes = [vp]
+    lib.pg_synth_free.restype = None
+
+
+_lib = None
+
+
+def _synth_lib():
+    """The generator's own library (no CUDA library is loaded for it)."""
+    global _lib
+    if _lib is None:
+        lib = records.cdll("libpastis_synth.so")
+        declare(lib)
+        _lib = lib
+    return _lib
 
 
 class SynthCfg(ctypes.Structure):
@@ -41,7 +71,7 @@ class Workload:
     name: str
     seq: np.ndarray          # residue codes (0..19), concatenated
     offs: np.ndarray         # uint64, nseqs + 1
-    pairs: np.ndarray        # capi.PAIR_DTYPE
+    pairs: np.ndarray        # records.PAIR_DTYPE
     homolog: np.ndarray      # uint8 per pair
     spurious: np.ndarray     # uint8 per pair: no shared k-mer, random seed
     family: np.ndarray
@@ -49,7 +79,7 @@ class Workload:
 
     @property
     def ascii(self):
-        return capi.decode(self.seq)
+        return records.decode(self.seq)
 
     def lengths(self):
         return np.diff(self.offs).astype(np.int64)
@@ -74,6 +104,12 @@ PRESETS = {
                       len_min=20, len_max=5000, mix_frac=0.2, mix_lo=1000, mix_hi=5000,
                       id_lo=0.30, id_hi=0.80, homolog_frac=0.5, k=6, alph=0, fam_min=6,
                       fam_max=6),
+    # the same batch, aligned by local Smith-Waterman (the X-drop and SW
+    # modes of the uneven-length workload)
+    "uneven10m_sw": dict(nseqs=2_000_000, npairs=10_000_000, len_median=300.0, len_sigma=0.5,
+                         len_min=20, len_max=5000, mix_frac=0.2, mix_lo=1000, mix_hi=5000,
+                         id_lo=0.30, id_hi=0.80, homolog_frac=0.5, k=6, alph=0, fam_min=6,
+                         fam_max=6),
     "manytomany": dict(nseqs=1_000_000, npairs=1_000, len_median=250.0, len_sigma=0.5,
                        len_min=30, len_max=1000, mix_frac=0.0, mix_lo=0, mix_hi=0, id_lo=0.30,
                        id_hi=0.90, homolog_frac=0.5, k=6, alph=0, fam_min=2, fam_max=50),
@@ -96,7 +132,7 @@ def generate(preset="xdrop1m", seed=20260101, scale=1.0, **over):
         setattr(c, k, p[k])
     c.indel_rate = p.get("indel_rate", 0.02)
     c.indel_mean = p.get("indel_mean", 3.0)
-    lib = capi.load("libpastis_synth.so")
+    lib = _synth_lib()
     h = lib.pg_synth_generate(ctypes.byref(c))
     if not h:
         raise MemoryError("synthetic generator failed")
@@ -111,7 +147,7 @@ def generate(preset="xdrop1m", seed=20260101, scale=1.0, **over):
 
         w = Workload(preset, arr(lib.pg_synth_seq(h), np.uint8, nres),
                      arr(lib.pg_synth_offs(h), np.uint64, ns + 1),
-                     arr(lib.pg_synth_pairs(h), capi.PAIR_DTYPE, npairs),
+                     arr(lib.pg_synth_pairs(h), records.PAIR_DTYPE, npairs),
                      arr(lib.pg_synth_homolog(h), np.uint8, npairs),
                      arr(lib.pg_synth_spurious(h), np.uint8, npairs),
                      arr(lib.pg_synth_family(h), np.uint32, ns),

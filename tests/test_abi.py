@@ -78,3 +78,20 @@ def test_create_rejects_bad_config(native):
         c = capi.config(capi.MODE_XDROP)
         setattr(c, field, val)
         assert lib.pg_create(ctypes.byref(c), ctypes.byref(h)) == capi.PG_ERR_ARG, field
+
+
+def test_noalloc_argument_checks_without_gpu(native):
+    """pg_align_sw_noalloc rejects a batch its 32-bit work counter cannot
+    index, and a column bound over 65535, before it touches a device."""
+    from pastis_gb300 import capi
+    lib = capi.load()
+    cfg = capi.config(capi.MODE_SW)
+    fake = 4096    # never dereferenced: the checks come first
+
+    def call(max_col, n):
+        return lib.pg_align_sw_noalloc(ctypes.byref(cfg), fake, fake, 1, fake, fake, 1, max_col,
+                                       fake, n, 0, 0, fake, None)
+
+    assert call(100, 1 << 31) == capi.PG_ERR_ARG
+    assert call(65536, 10) == capi.PG_ERR_RANGE
+    assert call(100, 0) == capi.PG_OK

@@ -238,6 +238,16 @@ def test_cpp_driver_on_gpu(sw_small, oracle_mod):
     assert st["nnz_aln"] == st2["nnz_aln"] and st["batches"] == 4
     assert (r_gpu == r_cpu).all() and (c_gpu == c_cpu).all()
     assert (v_gpu["score_aln"].view(np.uint32) == v_cpu["score_aln"].view(np.uint32)).all()
+    # stopped on the host after batch 1 and resumed from batch 2 with the GPU
+    # aligner: the same final triples
+    r1, c1, v1, s1 = capi.pw_aln_batch(capi.MODE_XDROP, rows, cols, vals, w.ascii, w.offs,
+                                      batch_sz=400, ckthr=0, cfg=cfg,
+                                      on_batch=lambda b, beg, end: b < 1)
+    assert s1["next_batch"] == 2 and not s1["complete"]
+    r2, c2, v2, s2 = capi.pw_aln_batch(capi.MODE_XDROP, r1, c1, v1, w.ascii, w.offs,
+                                      batch_sz=400, ckthr=0, cfg=cfg, start_batch=2)
+    assert s2["complete"] and (r2 == r_gpu).all() and (c2 == c_gpu).all()
+    assert v2.tobytes() == v_gpu.tobytes()
 
 
 @pytest.mark.parametrize("mode", [0, 1])

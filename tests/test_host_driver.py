@@ -121,3 +121,97 @@ def test_matrix_market_writer(native, tmp_path):
     assert np.array_equal(np.array([float(v) for _, _, v in got], dtype=np.float32), vals)
     with pytest.raises(capi.PgError):
         capi.write_mm(path, 10, 12, [10], [0], [1.0])
+
+
+def _xdrop_block(O, seed=3):
+    from pastis_gb300 import capi
+    res, offs, rows, cols, rng = _block(seed=seed, nnz=400)
+    vals = np.zeros(len(rows), dtype=capi.KMERLOC_DTYPE)
+    vals["count"] = rng.integers(1, 4, len(rows))
+    vals["score"] = rng.integers(-1, 30, len(rows))
+    L = np.diff(offs).astype(int)
+    vals["first_r"] = [rng.integers(0, L[r] - 6) for r in rows]
+    vals["first_c"] = [rng.integers(0, L[c] - 6) for c in cols]
+    return res, offs, rows, cols, vals
+
+
+@pytest.mark.parametrize("stop_after", [1, 3, 5])
+def test_resume_after_a_stop_between_batches(native, oracle_mod, stop_after):
+    """The run is stopped on the host after batch k (as a job stopped between
+    batches); a second call from next_batch on the written-back triples ends
+    with the LocalMat an uninterrupted run gives."""
+    from pastis_gb300 import capi
+    O = oracle_mod
+    res, offs, rows, cols, vals = _xdrop_block(O)
+    p = O.make_params(gap_first=-2, gap_ext=-11, xdrop_gap=-11)
+    cb = _oracle_cb(O, 1, res, offs, p)
+    kw = dict(batch_sz=40, ckthr=1, mosthr=3.0, callback=cb)
+    full = capi.pw_aln_batch(capi.MODE_XDROP, rows, cols, vals, res, offs, **kw)
+    assert full[3]["complete"] and full[3]["next_batch"] == full[3]["batches"]
+    seen = []
+
+    def stop(b, beg, end):
+        seen.append((b, beg, end))
+        return b + 1 < stop_after
+
+    r1, c1, v1, s1 = capi.pw_aln_batch(capi.MODE_XDROP, rows, cols, vals, res, offs,
+                                      on_batch=stop, **kw)
+    assert not s1["complete"] and s1["next_batch"] == stop_after
+    assert seen[-1][0] == stop_after - 1 and s1["last_end"] == seen[-1][2] == 40 * stop_after
+    # nothing after the k-mer prune ran: every surviving nonzero is still there
+    assert s1["nnz_aln"] == s1["nnz_kmer_thr"] == len(r1)
+    aligned = v1["score_aln"][:s1["last_end"]]
+    assert (v1["score_aln"][s1["last_end"]:] == 0).all() and (aligned != 0).any()
+    r2, c2, v2, s2 = capi.pw_aln_batch(capi.MODE_XDROP, r1, c1, v1, res, offs,
+                                      start_batch=s1["next_batch"], **kw)
+    assert s2["complete"] and s2["batches"] == full[3]["batches"] - stop_after
+    assert (r2 == full[0]).all() and (c2 == full[1]).all()
+    assert v2.tobytes() == full[2].tobytes()
+
+
+def test_failed_batch_surfaces_its_code_and_keeps_earlier_batches(native, oracle_mod):
+    """An aligner error in batch 2 (the host-side stand-in for a failed upload
+    or a failed pg_align) returns its code; batches 0 and 1 keep their
+    score_aln, and a resume from batch 2 completes the stage."""
+    from pastis_gb300 import capi
+    O = oracle_mod
+    res, offs, rows, cols, vals = _xdrop_block(O, seed=4)
+    p = O.make_params(gap_first=-2, gap_ext=-11, xdrop_gap=-11)
+    good = _oracle_cb(O, 1, res, offs, p)
+    calls = []
+
+    def flaky(pairs, ro, co):
+        calls.append(len(pairs))
+        if len(calls) == 3:
+            return capi.PG_ERR_CUDA
+        return good(pairs, ro, co)
+
+    kw = dict(batch_sz=50, ckthr=1, mosthr=3.0)
+    full = capi.pw_aln_batch(capi.MODE_XDROP, rows, cols, vals, res, offs, callback=good, **kw)
+    with pytest.raises(capi.BatchError) as ei:
+        capi.pw_aln_batch(capi.MODE_XDROP, rows, cols, vals, res, offs, callback=flaky, **kw)
+    e = ei.value
+    assert e.code == capi.PG_ERR_CUDA
+    r1, c1, v1, s1 = e.partial
+    assert s1["next_batch"] == 2 and s1["last_end"] == 100 and not s1["complete"]
+    # the earlier batches' results equal the uninterrupted run's for the same entries
+    ref = capi.pw_aln_batch(capi.MODE_XDROP, rows, cols, vals, res, offs, callback=good,
+                            on_batch=lambda b, beg, end: b < 1, **kw)
+    assert v1[:100].tobytes() == ref[2][:100].tobytes()
+    r2, c2, v2, s2 = capi.pw_aln_batch(capi.MODE_XDROP, r1, c1, v1, res, offs, callback=good,
+                                      start_batch=2, **kw)
+    assert s2["complete"] and v2.tobytes() == full[2].tobytes()
+    assert (r2 == full[0]).all() and (c2 == full[1]).all()
+
+
+def test_callback_exception_is_a_state_error(native, oracle_mod):
+    from pastis_gb300 import capi
+    res, offs, rows, cols, vals = _xdrop_block(oracle_mod, seed=5)
+
+    def boom(pairs, ro, co):
+        raise ValueError("host-side failure")
+
+    with pytest.raises(capi.BatchError) as ei:
+        capi.pw_aln_batch(capi.MODE_XDROP, rows, cols, vals, res, offs, callback=boom,
+                          batch_sz=64)
+    assert ei.value.code == capi.PG_ERR_STATE and ei.value.partial[3]["next_batch"] == 0
