@@ -190,13 +190,16 @@ typedef struct pg_tuning {
                                    of up to 32 * rows_max rows two per warp, each on half
                                    of it; no graph capture in these forms */
     int32_t dir_arena_mb;       /* cap on that arena in MiB; 0 = a third of the device memory */
-    int32_t xd_stepped;         /* X-drop extension, a thread per (pair, seed): 1 steps one
-                                   extension direction at a time and starts the next the
-                                   moment one ends; 0 runs each task to its end (fewer
-                                   registers, more resident warps); -1 picks 1 while the
-                                   resident sequences fit half of L2, else 0 (measured:
-                                   1 faster with sequences in L2, 0 when they stream
-                                   from DRAM) */
+    int32_t xd_stepped;         /* X-drop extension kernel, a thread per (pair, seed):
+                                   2 holds the band's 16-column window in registers and
+                                   computes it branch-free with packed 16-bit operations
+                                   (needs a linear X-drop gap of -1..-4096 and xdrop
+                                   <= 8192, else 1 runs); 1 steps one extension direction
+                                   at a time over a shared-memory ring and starts the next
+                                   the moment one ends; 0 runs each task to its end over
+                                   the ring (fewer registers, more resident warps);
+                                   -1 picks 2 where it applies, else 1 while the resident
+                                   sequences fit half of L2, else 0 */
 } pg_tuning;                    /* 36 bytes */
 
 /* The built-in tuning.  A new context starts from it with dp_traceback = 3

@@ -26,7 +26,8 @@ GRID = {
     "dp_blocks_per_sm": (1, 0),      # 0 = occupancy limit (2 on GB300)
     "xd_blocks_per_sm": (4, 0),      # 0 = occupancy limit (7 on GB300)
     "bucket_order": (1, 0),
-    "xd_stepped": (1, 0),            # X-drop extension: a direction per step, or run to end
+    "xd_stepped": (2, 1, 0),         # X-drop extension: register window, ring a direction per
+                                     # step, ring run to end
     "dp_traceback": (3, 0),          # 3 = traceback form on 16-bit lanes, 0 = statistics
 }
 
@@ -117,7 +118,7 @@ def tune(ctx, run, key=None, device=0, reps=3, grid=None, use_cache=True, log=No
               "candidates": len(rows), "validated_on_full_batch": validated, "default_ms": next(
                   (m for m, c in rows if c == {"dp_blocks_per_sm": 0, "xd_blocks_per_sm": 0,
                                                "bucket_order": 1, "graph": 0,
-                                               "xd_stepped": 1, "dp_traceback": 3}),
+                                               "xd_stepped": 2, "dp_traceback": 3}),
                   None)}
     if entry:
         try:

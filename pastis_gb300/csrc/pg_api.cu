@@ -121,6 +121,7 @@ struct pg_ctx {
     int grid = 0;                  // persistent blocks of the warp-per-pair kernel
     int grid_xd = 0;               // persistent blocks of k_xdf
     int grid_xd_run = 0;           // persistent blocks of k_xd
+    int grid_xdr = 0;              // persistent blocks of k_xdr
     uint64_t l2_bytes = 0;         // the device's L2 cache
     int grid_wide = 0;             // blocks of k_xd_wide
     Side side[2];
@@ -321,6 +322,9 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
         int pr = 0;
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pr, pg::k_xd, pg::XT, 0));
         c->grid_xd_run = c->nsm * std::max(pr, 1);
+        int pq = 0;
+        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pq, pg::k_xdr, pg::XT, 0));
+        c->grid_xdr = c->nsm * std::max(pq, 1);
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pw, pg::k_xd_wide, pg::WARPS * 32, 0));
         c->grid_xd = c->nsm * std::max(px, 1);
         c->grid_wide = c->nsm * std::max(pw, 1);
@@ -591,19 +595,26 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
     const int gsched = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (n + 255) / 256);
     CU(record_event(c, c->ev[0], st));
     if (c->cfg.mode == PG_MODE_XDROP) {
-        // extension kernel: k_xdf (a direction per step, the next task read
-        // ahead) while the resident sequences fit half of L2; k_xd (each task
-        // run to its end, more resident warps) when residues stream from DRAM
+        // extension kernel: k_xdr (the band window in registers) where the gap
+        // and X allow it; otherwise k_xdf (a direction per step, the next
+        // task read ahead) while the resident sequences fit half of L2, k_xd
+        // (each task run to its end, more resident warps) when residues
+        // stream from DRAM
         const uint64_t nres = c->side[0].nres + (c->cols_share_rows ? 0 : c->side[1].nres);
-        const bool stepped = c->tune.xd_stepped >= 0 ? c->tune.xd_stepped != 0 : nres <= c->l2_bytes / 2;
+        const bool reg_ok = pg::xdr_supported(kp.xg, c->cfg.xdrop);
+        int form = c->tune.xd_stepped;
+        if (form < 0) form = reg_ok ? 2 : (nres <= c->l2_bytes / 2 ? 1 : 0);
+        if (form == 2 && !reg_ok) form = 1;
         const bool int16 = c->tune.xd_int16 && c->cfg.xdrop <= pg::XMAX16;
         const uint64_t need_xd = (2 * n + pg::XT - 1) / pg::XT;
-        uint64_t xmax = (uint64_t)((stepped && !int16) ? c->grid_xd : c->grid_xd_run);
+        uint64_t xmax = (uint64_t)(int16 ? c->grid_xd_run
+                                         : form == 2 ? c->grid_xdr : form == 1 ? c->grid_xd : c->grid_xd_run);
         if (c->tune.xd_blocks_per_sm > 0)
             xmax = std::min<uint64_t>(xmax, (uint64_t)c->nsm * (uint64_t)c->tune.xd_blocks_per_sm);
         const int gx = (int)std::min<uint64_t>(xmax, need_xd);
         if (int16) pg::k_xd16<<<gx, pg::XT, 0, st>>>(kp);
-        else if (stepped) pg::k_xdf<<<gx, pg::XT, 0, st>>>(kp);
+        else if (form == 2) pg::k_xdr<<<gx, pg::XT, 0, st>>>(kp);
+        else if (form == 1) pg::k_xdf<<<gx, pg::XT, 0, st>>>(kp);
         else pg::k_xd<<<gx, pg::XT, 0, st>>>(kp);
         pg::k_xd_wide<<<c->grid_wide, blk, 0, st>>>(kp);
         if (kp.order) {
@@ -775,7 +786,7 @@ int pg_set_tuning(pg_ctx *c, const pg_tuning *t)
     if (t->xd_int16 != 0 && t->xd_int16 != 1) return fail(PG_ERR_ARG, "xd_int16 must be 0 or 1");
     if (t->dp_traceback < 0 || t->dp_traceback > 3) return fail(PG_ERR_ARG, "dp_traceback must be 0..3");
     if (t->dir_arena_mb < 0) return fail(PG_ERR_ARG, "dir_arena_mb must be >= 0");
-    if (t->xd_stepped < -1 || t->xd_stepped > 1) return fail(PG_ERR_ARG, "xd_stepped must be -1, 0 or 1");
+    if (t->xd_stepped < -1 || t->xd_stepped > 2) return fail(PG_ERR_ARG, "xd_stepped must be -1, 0, 1 or 2");
     c->tune = *t;
     ++c->epoch;                         // launch shapes changed: recapture
     return PG_OK;

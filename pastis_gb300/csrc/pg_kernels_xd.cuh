@@ -1,13 +1,16 @@
 // pg_kernels_xd.cuh -- the X-drop extension kernels (one definition: only
-// pg_api.cu includes this file): k_xdf and k_xd, thread per (pair, seed) task
-// with the 32-bit band (pg_xdrop.cuh), stepping one direction at a time or
-// running each task to its end (tuning option xd_stepped); k_xd16, a thread
-// per task on 16-bit lanes (tuning option xd_int16); k_xd_wide, warp per task
-// for the bands that overflow a thread's ring.
+// pg_api.cu includes this file): k_xdr, thread per (pair, seed) task with the
+// band window in registers (pg_xdreg.cuh), the default; k_xdf and k_xd,
+// thread per task with the 32-bit band in a shared-memory ring (pg_xdrop.cuh),
+// stepping one direction at a time or running each task to its end (tuning
+// option xd_stepped); k_xd16, a thread per task on 16-bit lanes (tuning option
+// xd_int16); k_xd_wide, warp per task for the bands that overflow a thread's
+// window or ring.
 #pragma once
 #include <cstdint>
 
 #include "pg_kernels.cuh"
+#include "pg_xdreg.cuh"
 
 namespace pg {
 
@@ -204,6 +207,134 @@ __global__ void __launch_bounds__(XT) k_xdf(const KParams kp)
             bv -= x.dv; bh -= x.dh;
             if (ev < m && eh < n) {
                 dir.init(V + ev, m - ev, 1, Hs + eh, n - eh, 1, kp.xg, kp.xdrop, base);
+                phase = 2;
+            } else {
+                write_rec();
+                phase = 0;
+            }
+        } else {
+            ev += x.dv; eh += x.dh;
+            write_rec();
+            phase = 0;
+        }
+    }
+    if (exec) atomicAdd(kp.exec_cells, exec);
+}
+
+// ------------------------------------------------------------------ k_xdr
+// One thread per (pair, seed) task with the band window in registers
+// (XrDir): every step computes the 16 window columns with packed 16-bit
+// operations and no branch on the band, so a warp's threads step together
+// whatever their band widths.  Tasks are taken and their inputs read ahead as
+// in k_xdf; a direction starts the moment the previous one ends.  A window
+// wider than 15 columns sends the task to the overflow list for k_xd_wide.
+// Needs xdr_supported(xg, xdrop).
+__global__ void __launch_bounds__(XT) k_xdr(const KParams kp)
+{
+    __shared__ int ssm[PG_NRES * XR_STRIDE];
+    load_sm33(ssm, kp.sm);
+    __syncthreads();
+    const char *tbl = reinterpret_cast<const char *>(ssm);
+    const uint32_t ntask = (uint32_t)(2 * kp.n);
+    unsigned long long exec = 0;
+    uint32_t ta, tb;
+    pg_pair pb;
+    XfReady c;
+    auto load_pair = [&](uint32_t t, pg_pair &pr) {
+        if (t < ntask) pr = kp.pairs[t >> 1];
+    };
+    auto make_ready = [&](uint32_t t, const pg_pair &pr, XfReady &x) {
+        x.t = t;
+        x.flags = 0;
+        if (t >= ntask) return;
+        x.flags = XFT_VALID;
+        const uint64_t r = (uint64_t)pr.row + kp.roff, cc = (uint64_t)pr.col + kp.coff;
+        const int s = (int)(t & 1);
+        x.seed = s ? ((uint32_t)pr.rs1 | ((uint32_t)pr.cs1 << 16)) : ((uint32_t)pr.rs0 | ((uint32_t)pr.cs0 << 16));
+        if (pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) x.flags |= XFT_SAME;
+        if (pr.count < 2) x.flags |= XFT_FEW;
+        if (r >= kp.nr || cc >= kp.nc) return;
+        x.flags |= XFT_IDX;
+        x.r0 = kp.roffs[r]; x.r1 = kp.roffs[r + 1];
+        x.c0 = kp.coffs[cc]; x.c1 = kp.coffs[cc + 1];
+    };
+    {
+        const uint32_t t0 = atomicAdd(&kp.counter[1], 1u);
+        pg_pair p0;
+        load_pair(t0, p0);
+        make_ready(t0, p0, c);
+        tb = atomicAdd(&kp.counter[1], 1u);
+        load_pair(tb, pb);
+        ta = atomicAdd(&kp.counter[1], 1u);
+    }
+
+    XrDir dir;
+    XdRec rec{0, 0, 0, 0, 0u, 0u};
+    uint32_t task = 0;
+    const uint8_t *V = nullptr, *Hs = nullptr;
+    int m = 0, n = 0, bv = 0, ev = 0, bh = 0, eh = 0;
+    int phase = 0;     // 0: start a task, 1: left direction running, 2: right direction running
+    auto write_rec = [&]() {
+        if (rec.flags & XF_OVF) {
+            rec.cells = 0;
+            const unsigned int slot = atomicAdd(&kp.counter[2], 1u);
+            kp.ovf[slot] = task;
+        } else if (!(rec.flags & (XF_NONE | XF_SAME | XF_BADIDX))) {
+            rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev;
+            rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
+            exec += rec.cells;
+        }
+        kp.xd[task] = rec;
+    };
+    for (;;) {
+        while (phase == 0) {
+            if (!(c.flags & XFT_VALID)) break;
+            const XfReady cur = c;
+            make_ready(tb, pb, c);
+            tb = ta;
+            load_pair(tb, pb);
+            ta = atomicAdd(&kp.counter[1], 1u);
+            task = cur.t;
+            const int s = (int)(task & 1);
+            rec = XdRec{0, 0, 0, 0, 0u, 0u};
+            if (!(cur.flags & XFT_IDX)) {
+                rec.flags = XF_BADIDX;
+            } else if (s >= kp.seed_count ||
+                       (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && (cur.flags & XFT_FEW))) {
+                rec.flags = XF_NONE;
+            } else if (s == 1 && (cur.flags & XFT_SAME)) {
+                rec.flags = XF_SAME;
+            } else {
+                V = kp.rseq + cur.r0; m = (int)(cur.r1 - cur.r0);
+                Hs = kp.cseq + cur.c0; n = (int)(cur.c1 - cur.c0);
+                bv = (int)(cur.seed & 0xffffu); bh = (int)(cur.seed >> 16);
+                ev = bv + kp.seed_len; eh = bh + kp.seed_len;
+                if (ev > m || eh > n) {
+                    bv = min(bv, m); ev = min(ev, m); bh = min(bh, n); eh = min(eh, n);
+                    rec.flags |= XF_BAD;
+                }
+                if (bv > 0 && bh > 0) {
+                    dir.init(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1, kp.xg, kp.xdrop);
+                    phase = 1;
+                } else if (ev < m && eh < n) {
+                    dir.init(V + ev, m - ev, 1, Hs + eh, n - eh, 1, kp.xg, kp.xdrop);
+                    phase = 2;
+                }
+            }
+            if (phase == 0) write_rec();
+        }
+        if (phase == 0) break;
+        if (dir.step(tbl, kp.xg, kp.xdrop)) continue;
+        const XdOut x = dir.finish();
+        rec.cells += x.cells;
+        if (!x.ok) {
+            rec.flags |= XF_OVF;
+            write_rec();
+            phase = 0;
+        } else if (phase == 1) {
+            bv -= x.dv; bh -= x.dh;
+            if (ev < m && eh < n) {
+                dir.init(V + ev, m - ev, 1, Hs + eh, n - eh, 1, kp.xg, kp.xdrop);
                 phase = 2;
             } else {
                 write_rec();

@@ -29,7 +29,7 @@ def test_search_picks_fastest_and_caches(native, tmp_path, monkeypatch):
     assert best["dp_blocks_per_sm"] == 0 and best["bucket_order"] == 1
     assert best["graph"] == 1
     assert ctx.t["graph"] == 1 and not rep["cached"]
-    assert rep["candidates"] == 32
+    assert rep["candidates"] == 48
     ctx2 = FakeCtx()
     best2, rep2 = autotune.tune(ctx2, lambda: None, key="k1")
     assert rep2["cached"] and best2 == best and ctx2.t["dp_traceback"] == 0

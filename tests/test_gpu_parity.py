@@ -274,7 +274,7 @@ def test_tuning_and_graph_replay_keep_results(native, oracle_mod, mode):
               {"dp_traceback": 2, "dir_arena_mb": 1}, {"dp_traceback": 2, "rows_max": 3},
               {"dp_traceback": 2, "bucket_order": 0}, {"dp_traceback": 3},
               {"dp_traceback": 3, "dir_arena_mb": 1}, {"dp_traceback": 3, "rows_max": 3},
-              {"dp_traceback": 3, "bucket_order": 0}, {"xd_stepped": 0}, {"xd_stepped": 1},
+              {"dp_traceback": 3, "bucket_order": 0}, {"xd_stepped": 0}, {"xd_stepped": 1}, {"xd_stepped": 2},
               {"xd_stepped": 0, "xd_blocks_per_sm": 2}):
         ctx.set_tuning(capi.default_tuning(), **t)
         for rep in range(2):                 # the second call replays the graph

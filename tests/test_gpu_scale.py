@@ -81,7 +81,7 @@ def test_long_smith_waterman_pairs(native, oracle_mod):
     assert (got["flags"] & capi.RF_PASSED).any()
 
 
-@pytest.mark.parametrize("stepped", [-1, 0, 1])
+@pytest.mark.parametrize("stepped", [-1, 0, 1, 2])
 def test_xdrop_residues_beyond_l2(native, oracle_mod, stepped):
     """A residue set of about 90 MB (more than half of L2, where the default
     picks the run-to-end extension kernel) under each extension form."""
