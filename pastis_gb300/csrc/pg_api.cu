@@ -140,6 +140,7 @@ struct pg_ctx {
     uint32_t *d_ovf = nullptr;          // overflowed extension tasks
     uint64_t xd_cap = 0;
     uint32_t *d_order = nullptr;        // bucket order of the pairs
+    uint32_t *d_xorder = nullptr;       // X-drop extension tasks, longest length bound first
     uint64_t order_cap = 0;
     // traceback form: direction arena, per-task byte counts / offsets,
     // per-pair scores and end cells, scan scratch
@@ -235,6 +236,7 @@ void pg_destroy(pg_ctx *ctx)
     cudaFree(ctx->d_xd);
     cudaFree(ctx->d_ovf);
     cudaFree(ctx->d_order);
+    cudaFree(ctx->d_xorder);
     cudaFree(ctx->d_dir); cudaFree(ctx->d_dbytes); cudaFree(ctx->d_doff); cudaFree(ctx->d_t1);
     cudaFree(ctx->d_dsc); cudaFree(ctx->d_scan);
     cudaFree(ctx->d_pairs);
@@ -295,7 +297,7 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
     CUD(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CUD(cudaMalloc(&c->d_sm, sizeof c->sm));
     CUD(cudaMemcpy(c->d_sm, c->sm, sizeof c->sm, cudaMemcpyHostToDevice));
-    CUD(cudaMalloc(&c->d_counter, (4 + pg::SCHED_WORDS) * sizeof(unsigned int)));
+    CUD(cudaMalloc(&c->d_counter, (4 + pg::SCHED_WORDS + pg::XSCHED_WORDS) * sizeof(unsigned int)));
     CUD(cudaMalloc(&c->d_status, sizeof(int)));
     CUD(cudaMalloc(&c->d_exec, 2 * sizeof(unsigned long long)));
     CUD(cudaMemset(c->d_exec, 0, 2 * sizeof(unsigned long long)));
@@ -396,11 +398,12 @@ static int ensure_batch(pg_ctx *c, uint64_t n)
         c->order_cap = n;
     }
     if (c->cfg.mode != PG_MODE_XDROP || n <= c->xd_cap) return PG_OK;
-    cudaFree(c->d_xd); cudaFree(c->d_ovf);
-    c->d_xd = nullptr; c->d_ovf = nullptr; c->xd_cap = 0;
+    cudaFree(c->d_xd); cudaFree(c->d_ovf); cudaFree(c->d_xorder);
+    c->d_xd = nullptr; c->d_ovf = nullptr; c->d_xorder = nullptr; c->xd_cap = 0;
     ++c->epoch;
     CU(cudaMalloc(&c->d_xd, 2 * n * sizeof(pg::XdRec)));
     CU(cudaMalloc(&c->d_ovf, 2 * n * sizeof(uint32_t)));
+    CU(cudaMalloc(&c->d_xorder, 2 * n * sizeof(uint32_t)));
     c->xd_cap = n;
     return PG_OK;
 }
@@ -572,6 +575,7 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
     kp.gring = c->d_gring; kp.gring_w = c->gring_w;
     kp.sched = c->d_counter + 4;
     kp.order = c->tune.bucket_order ? c->d_order : nullptr;
+    kp.xsched = c->d_counter + 4 + pg::SCHED_WORDS;
     kp.rows_cap = c->tune.rows_max;
     kp.dir = c->tune.dp_traceback ? 1 : 0;
     kp.dir16_lim = c->tune.dp_traceback >= 2 ? c->lim16 : 0;
@@ -584,7 +588,7 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         if (c->cfg.mode == PG_MODE_SW || gmax >= 0) kp.dir16_side = 65535;
         else kp.dir16_side = std::min(65535, (pg::SAT16_DP - std::abs(c->go)) / -gmax);
     }
-    CU(cudaMemsetAsync(c->d_counter, 0, (4 + pg::SCHED_WORDS) * sizeof(unsigned int), st));
+    CU(cudaMemsetAsync(c->d_counter, 0, (4 + pg::SCHED_WORDS + pg::XSCHED_WORDS) * sizeof(unsigned int), st));
     CU(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
     const uint64_t need_blocks = (n + pg::WARPS - 1) / pg::WARPS;
     uint64_t gmax = (uint64_t)c->grid;
@@ -612,6 +616,17 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         if (c->tune.xd_blocks_per_sm > 0)
             xmax = std::min<uint64_t>(xmax, (uint64_t)c->nsm * (uint64_t)c->tune.xd_blocks_per_sm);
         const int gx = (int)std::min<uint64_t>(xmax, need_xd);
+        int xlaunch = 0;
+        if (!int16 && form == 2 && c->tune.bucket_order) {
+            // the extension tasks longest length bound first
+            pg::KParams ko = kp;
+            ko.xorder = c->d_xorder;
+            const int gord = (int)std::min<uint64_t>((uint64_t)c->nsm * 8, (n + 255) / 256);
+            pg::k_xtask_hist<<<gord, 256, 0, st>>>(ko);
+            pg::k_xtask_bucket<<<gord, 256, 0, st>>>(ko);
+            kp.xorder = c->d_xorder;
+            xlaunch = 2;
+        }
         if (int16) pg::k_xd16<<<gx, pg::XT, 0, st>>>(kp);
         else if (form == 2) pg::k_xdr<<<gx, pg::XT, 0, st>>>(kp);
         else if (form == 1) pg::k_xdf<<<gx, pg::XT, 0, st>>>(kp);
@@ -626,10 +641,10 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         if (kp.dir) {
             const int l = run_dir(c, kp, n, (int)gmax, st);
             if (l < 0) return l;
-            c->last_launches = (kp.order ? 4 : 2) + l;
+            c->last_launches = (kp.order ? 4 : 2) + l + xlaunch;
         } else {
             pg::stat_run(true, c->cfg.tie, kp, grid, dyn, st);
-            c->last_launches = kp.order ? 5 : 3;
+            c->last_launches = (kp.order ? 5 : 3) + xlaunch;
         }
     } else {
         if (kp.order) {

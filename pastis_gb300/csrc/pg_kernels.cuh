@@ -86,6 +86,8 @@ struct KParams {
     int dir16_lim = 0;               // traceback form: regions with m + n <= this on 16-bit lanes
     int dir16_side = 0;              // ... and larger ones with both sides <= this, checked
     int dir16_pair = 0;              // 1: 16-bit regions of up to 32 x rows_cap rows two per warp
+    const uint32_t *xorder = nullptr; // X-drop extension tasks, longest length bound first (null: t)
+    unsigned int *xsched = nullptr;   // [0, XBUCKET) task bucket sizes, [XBUCKET, 2*XBUCKET) cursors
 };
 
 __device__ __forceinline__ void load_sm(int *ssm, const int8_t *sm)
@@ -222,6 +224,8 @@ __device__ __forceinline__ DpOut<S> dp_dispatch(const uint8_t *V, int m, const u
 // fill the tail of the batch.
 constexpr int NBUCKET = 24;
 constexpr int SCHED_WORDS = 2 * NBUCKET;
+constexpr int XBUCKET = 72;          // extension task buckets: quarter octaves of the length bound
+constexpr int XSCHED_WORDS = 2 * XBUCKET;
 constexpr int BUCKET_NONE = 23;   // no DP work
 
 // traceback form, lanes of a region's DP (pg_dpdir16.cuh): 0 32-bit; 1 16-bit,

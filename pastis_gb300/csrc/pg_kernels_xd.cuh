@@ -221,6 +221,97 @@ __global__ void __launch_bounds__(XT) k_xdf(const KParams kp)
     if (exec) atomicAdd(kp.exec_cells, exec);
 }
 
+// --------------------------------------------------- extension task order
+// Threads take extension tasks from a shared counter, so a thread that picks
+// up a long task near the end of the batch leaves its warp's other lanes
+// idle until it finishes.  Taking the tasks longest first fixes that: their
+// length is not known beforehand, but the anti-diagonals a seed's two
+// directions can reach are bounded by the residues left of it and right of
+// it on both sequences, and ordering by that bound (in quarter octaves)
+// gives nearly the ideal finish (a simulation over task lengths of this
+// workload: 1.01 of the mean thread load against 1.23 in input order).
+// Tasks that run no extension (a second seed equal to the first, or switched
+// off) sit in bucket 0, last.
+__device__ __forceinline__ int xtask_bucket(const KParams &kp, const pg_pair &pr, int s, int m, int n)
+{
+    if (s >= kp.seed_count || (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0)) return 0;
+    const int rs = s ? pr.rs1 : pr.rs0, cs = s ? pr.cs1 : pr.cs0;
+    const int left = max(0, min(min(rs, cs), min(m, n)));
+    const int right = max(0, min(m - rs - kp.seed_len, n - cs - kp.seed_len));
+    const uint32_t b = (uint32_t)(left + right) + 2u;    // >= 2
+    const int e = 31 - __clz(b);
+    const int q = 4 * e + (int)((b << 2 >> e) & 3u);
+    return min(XBUCKET - 1, q);
+}
+
+// the two tasks of pair p and their buckets (both 0 when the pair's indices
+// are out of range: the extension kernel reports those itself)
+__device__ __forceinline__ void xtask_buckets(const KParams &kp, uint64_t p, int &b0, int &b1)
+{
+    const pg_pair pr = kp.pairs[p];
+    const uint64_t r = (uint64_t)pr.row + kp.roff, c = (uint64_t)pr.col + kp.coff;
+    b0 = b1 = 0;
+    if (r >= kp.nr || c >= kp.nc) return;
+    const int m = (int)(kp.roffs[r + 1] - kp.roffs[r]), n = (int)(kp.coffs[c + 1] - kp.coffs[c]);
+    b0 = xtask_bucket(kp, pr, 0, m, n);
+    b1 = xtask_bucket(kp, pr, 1, m, n);
+}
+
+__global__ void __launch_bounds__(256) k_xtask_hist(const KParams kp)
+{
+    __shared__ unsigned int h[XBUCKET];
+    for (int b = threadIdx.x; b < XBUCKET; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < kp.n;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        int b0, b1;
+        xtask_buckets(kp, p, b0, b1);
+        atomicAdd(&h[b0], 1u);
+        atomicAdd(&h[b1], 1u);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < XBUCKET; b += blockDim.x)
+        if (h[b]) atomicAdd(&kp.xsched[b], h[b]);
+}
+
+// xorder[]: task ids, highest bucket first (any order inside a bucket)
+__global__ void __launch_bounds__(256) k_xtask_bucket(const KParams kp)
+{
+    __shared__ unsigned int start[XBUCKET], h[XBUCKET], base[XBUCKET];
+    if (threadIdx.x == 0) {
+        unsigned int acc = 0;
+        for (int b = XBUCKET - 1; b >= 0; --b) { start[b] = acc; acc += kp.xsched[b]; }
+    }
+    uint32_t *order = const_cast<uint32_t *>(kp.xorder);
+    const uint64_t ntask = 2 * kp.n;
+    for (uint64_t c0 = (uint64_t)blockIdx.x * blockDim.x; c0 < kp.n; c0 += (uint64_t)gridDim.x * blockDim.x) {
+        for (int b = threadIdx.x; b < XBUCKET; b += blockDim.x) h[b] = 0;
+        __syncthreads();
+        const uint64_t p = c0 + threadIdx.x;
+        int b0 = 0, b1 = 0;
+        unsigned int r0 = 0, r1 = 0;
+        if (p < kp.n) {
+            xtask_buckets(kp, p, b0, b1);
+            r0 = atomicAdd(&h[b0], 1u);
+            r1 = atomicAdd(&h[b1], 1u);
+        }
+        __syncthreads();
+        for (int b = threadIdx.x; b < XBUCKET; b += blockDim.x)
+            if (h[b]) base[b] = start[b] + atomicAdd(&kp.xsched[XBUCKET + b], h[b]);
+        __syncthreads();
+        if (p < kp.n) {
+            const uint64_t q0 = (uint64_t)base[b0] + r0, q1 = (uint64_t)base[b1] + r1;
+            if (q0 < ntask && q1 < ntask) {
+                order[q0] = (uint32_t)(2 * p);
+                order[q1] = (uint32_t)(2 * p + 1);
+            } else {
+                atomicOr(kp.status, ST_BAD_SCHED);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------------ k_xdr
 // One thread per (pair, seed) task with the band window in registers
 // (XrDir): every step computes the 16 window columns with packed 16-bit
@@ -240,6 +331,11 @@ __global__ void __launch_bounds__(XT) k_xdr(const KParams kp)
     uint32_t ta, tb;
     pg_pair pb;
     XfReady c;
+    // the next task: through the longest-first order when there is one
+    auto fetch = [&]() -> uint32_t {
+        const uint32_t i = atomicAdd(&kp.counter[1], 1u);
+        return (kp.xorder && i < ntask) ? kp.xorder[i] : i;
+    };
     auto load_pair = [&](uint32_t t, pg_pair &pr) {
         if (t < ntask) pr = kp.pairs[t >> 1];
     };
@@ -259,13 +355,13 @@ __global__ void __launch_bounds__(XT) k_xdr(const KParams kp)
         x.c0 = kp.coffs[cc]; x.c1 = kp.coffs[cc + 1];
     };
     {
-        const uint32_t t0 = atomicAdd(&kp.counter[1], 1u);
+        const uint32_t t0 = fetch();
         pg_pair p0;
         load_pair(t0, p0);
         make_ready(t0, p0, c);
-        tb = atomicAdd(&kp.counter[1], 1u);
+        tb = fetch();
         load_pair(tb, pb);
-        ta = atomicAdd(&kp.counter[1], 1u);
+        ta = fetch();
     }
 
     XrDir dir;
@@ -293,7 +389,7 @@ __global__ void __launch_bounds__(XT) k_xdr(const KParams kp)
             make_ready(tb, pb, c);
             tb = ta;
             load_pair(tb, pb);
-            ta = atomicAdd(&kp.counter[1], 1u);
+            ta = fetch();
             task = cur.t;
             const int s = (int)(task & 1);
             rec = XdRec{0, 0, 0, 0, 0u, 0u};
