@@ -356,10 +356,18 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
 // rows per lane of a region on half a warp (m <= 256)
 __host__ __device__ __forceinline__ int dir16_pair_rows(int m) { return m > 32 ? (m + 31) / 32 : 1; }
 
+// Layout of a half-warp region: tiles of 4 wavefront steps; in a tile, each
+// lane's 8-byte words (its two virtual lanes) of the 4 steps make one 32-byte
+// sector: uint2 ((k / 4) * 16 + lane) * 4 + k % 4.  A traceback walk along a
+// lane then reads a new sector every few moves instead of at every move.
 __host__ __device__ __forceinline__ uint64_t dir16_pair_bytes(int m, int n)
 {
     if (m <= 0 || n <= 0) return 0;
-    return (uint64_t)(n + 31) * 128ull;
+    return (uint64_t)((n + 31 + 3) / 4) * 512ull;
+}
+__host__ __device__ __forceinline__ uint64_t dir16_pair_word(int k, int v)
+{
+    return ((uint64_t)((k >> 2) * 16 + (v >> 1)) * 4u + (uint64_t)(k & 3)) * 2u + (uint64_t)(v & 1);
 }
 
 // Each lane passes its half-warp's region (m = 0: none); R >= dir16_pair_rows(m)
@@ -431,7 +439,7 @@ __device__ DirOut dp_pair_dir16(const uint8_t *__restrict__ V, int m,
         const int j1 = -2 * sl + 1;
         if (j1 >= 1 && j1 <= n) hc_next = (int)__ldg(Hs + j1 - 1);
     }
-    uint2 *dstep = reinterpret_cast<uint2 *>(dir) + sl;
+    uint2 *dtile = reinterpret_cast<uint2 *>(dir) + sl * 4;
     uint32_t sbs = 0, sbs_seen = 0;
     int sbp0 = 0, sbp1 = 0;
     int nsteps = has ? n + v_last : 0;
@@ -483,7 +491,8 @@ __device__ DirOut dp_pair_dir16(const uint8_t *__restrict__ V, int m,
                 Gl[r] = G;
                 if (LOCAL) sbs = v16max(sbs, Hv);
             }
-            dstep[(uint64_t)k * 16u] = make_uint2(prmt(W0, W1, 0x5410u), prmt(W0, W1, 0x7632u));
+            dtile[(uint64_t)(k >> 2) * 64u + (uint64_t)(k & 3)] =
+                make_uint2(prmt(W0, W1, 0x5410u), prmt(W0, W1, 0x7632u));
             out_h = Hl[R - 1];
             out_a = cA;
             if (LOCAL && sbs != sbs_seen) {

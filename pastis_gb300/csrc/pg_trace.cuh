@@ -24,6 +24,7 @@
 
 #include "../../include/pastis_gb300.h"
 #include "pg_dpdir.cuh"
+#include "pg_dpdir16.cuh"
 
 namespace pg {
 
@@ -37,8 +38,9 @@ struct TraceOut {
 // carries the score of the cell it stands on, h, and stops where it is 0).
 // Otherwise the nibbles of dp_warp_dir (bits 0-1: diagonal, F, E or the local
 // floor).  Words: (s * (n + vl - 1) + k) * vl + v for stripe s, wavefront step
-// k = j - 1 + v, lane v (vl = 32 lanes, 64 virtual lanes of a warp, or 32 of a
-// half-warp).  ssm: the 32 x 32 substitution table in shared memory (read only
+// k = j - 1 + v, lane v (vl = 32 lanes or 64 virtual lanes of a warp); the
+// half-warp regions of dp_pair_dir16 (W16, vl = 32) lie in 4-step tiles
+// (dir16_pair_word).  ssm: the 32 x 32 substitution table in shared memory (read only
 // by a local W16 walk).  step() makes one move and returns false once the walk
 // has ended; the counts are then final.
 template <bool LOCAL, bool W16>
@@ -88,7 +90,9 @@ struct Walker {
         }
         // the word of (i, j) first (i, j >= 1 here): its load does not wait on h,
         // whose substitution-score lookups it overlaps
-        const uint32_t w = __ldg(dir + ((uint64_t)s * (uint64_t)(n + vl - 1) + (uint64_t)(j - 1 + v)) * (uint64_t)vl + v);
+        const uint64_t widx = (W16 && vl == 32) ? dir16_pair_word(j - 1 + v, v)
+                              : ((uint64_t)s * (uint64_t)(n + vl - 1) + (uint64_t)(j - 1 + v)) * (uint64_t)vl + v;
+        const uint32_t w = __ldg(dir + widx);
         if (W16 && LOCAL && state == 0 && h == 0) { done = true; return false; }
         const uint32_t nib = (w >> (4 * r)) & 15u;
         if (state == 0) {

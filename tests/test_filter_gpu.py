@@ -40,8 +40,11 @@ def test_forward_and_gradients_match_reference(native):
     for name, a, b in (("W1", M.P_W1, M.P_B1), ("b1", M.P_B1, M.P_W2), ("W2", M.P_W2, M.P_B2),
                        ("b2", M.P_B2, M.P_W3), ("w3", M.P_W3, M.P_B3), ("b3", M.P_B3, M.NPARAM)):
         gg, rr = g[a:b], g_ref[a:b]
+        # the kernels and the reference share every bf16 rounding point; what
+        # remains is the order of float32 sums (measured: about 1e-7 of the
+        # largest gradient), so an indexing slip on any weight shows here
         err = np.abs(gg - rr).max() / (np.abs(rr).max() + 1e-12)
-        assert err < 2e-2, (name, err)
+        assert err < 1e-5, (name, err)
     f.close()
 
 
@@ -95,8 +98,8 @@ def test_filtered_alignment_contract(native):
 
 def test_trained_filter_beats_kmer_prune(native):
     """Train on labels from this library's SW kernel; at >= 99.5 % recall of
-    the positives the network keeps fewer candidates than the best count or
-    k-mer-score threshold (PASTIS's own prune) at the same recall."""
+    the held-out positives the network keeps fewer candidates than the best
+    count or k-mer-score threshold (PASTIS's own prune) at the same recall."""
     import torch
     from pastis_gb300 import capi, synth
     from pastis_gb300 import filter as F
@@ -112,9 +115,11 @@ def test_trained_filter_beats_kmer_prune(native):
     probe = F.Filter(0, seed=1)
     probe.features(ctx, d_pairs.data_ptr(), n, feats.data_ptr())
     probe.close()
-    f, thr, m = F.train(w, feats, labels, epochs=4, recall=0.995)
-    assert m["val"]["recall"] >= 0.995
-    assert m["test"]["recall"] >= 0.98
+    # the threshold keeps 99.7 % of the validation positives so that the
+    # held-out test split stays at or above the 99.5 % target
+    f, thr, m = F.train(w, feats, labels, epochs=4, recall=0.997)
+    assert m["val"]["recall"] >= 0.997
+    assert m["test"]["recall"] >= 0.995
     assert m["test"]["kept_fraction"] < m["kmer_rule_kept_at_same_recall"]
     f.close()
     ctx.close()
