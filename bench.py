@@ -733,6 +733,22 @@ def gen_candidates(ctx, kc, rows, cols, dev, stream):
         return buf[:int(n.value) * capi.PAIR_DTYPE.itemsize], int(n.value)
 
 
+def count_candidates(ctx, kc, blocks, bounds, stream):
+    """Candidate pairs of the blocks under kc, counted without output."""
+    import ctypes
+    from pastis_gb300 import capi
+    tot = 0
+    for i, j in blocks:
+        n = ctypes.c_uint64()
+        rc = ctx.lib.pg_candidates(ctx.h, ctypes.byref(kc), int(bounds[i]), int(bounds[i + 1]),
+                                   int(bounds[j]), int(bounds[j + 1]), None, 0, ctypes.byref(n),
+                                   stream.cuda_stream)
+        if rc != capi.PG_OK and not (rc == capi.PG_ERR_RANGE and n.value > 0):
+            capi._check(rc)
+        tot += int(n.value)
+    return tot
+
+
 def run_manytomany(args, rank, world, local_rank):
     """Blocked many-to-many search: GPU k-mer SpGEMM candidates (k = 6,
     stride 1, even/odd symmetric prune, ckthr = 1) streamed in --bsz batches
@@ -782,6 +798,12 @@ def run_manytomany(args, rank, world, local_rank):
     sync()
     gen_s = time.perf_counter() - t0
     ncand = sum(c[3] for c in cand)
+    # the counts the reference logs per block, untimed: the product's nonzeros
+    # before any prune (c_nnz, src/sim_search.cpp:164-165) and after the
+    # symmetric prune (prune_sym, :189-190); ncand is after the ckthr prune too
+    prod_nnz, sym_nnz = (count_candidates(ctx, capi.kmer_config(k=6, stride=1, prune=pr, ckthr=0),
+                                          blocks, bounds, stream)
+                         for pr in (capi.PRUNE_NONE, capi.PRUNE_EVEN_ODD))
     bsz = args.bsz
     R = capi.RESULT_DTYPE.itemsize
     P = capi.PAIR_DTYPE.itemsize
@@ -859,13 +881,14 @@ def run_manytomany(args, rank, world, local_rank):
     f.close()
 
     stats = torch.tensor([gen_s, plain_s, filt_s], dtype=torch.float64, device=f"cuda:{dev}")
-    counts = torch.tensor([ncand, cells, ntrip, ftrip, plain_trip, kept_trip], dtype=torch.int64,
-                          device=f"cuda:{dev}")
+    counts = torch.tensor([ncand, cells, ntrip, ftrip, plain_trip, kept_trip, prod_nnz, sym_nnz],
+                          dtype=torch.int64, device=f"cuda:{dev}")
     if dist is not None:
         dist.all_reduce(stats, op=dist.ReduceOp.MAX)
         dist.all_reduce(counts)
     gen_s, plain_s, filt_s = (float(x) for x in stats.tolist())
-    ncand, cells, ntrip, ftrip, plain_trip, kept_trip = (int(x) for x in counts.tolist())
+    ncand, cells, ntrip, ftrip, plain_trip, kept_trip, prod_nnz, sym_nnz = (
+        int(x) for x in counts.tolist())
     if rank == 0:
         line = {
             "metric": METRIC, "value": cells / plain_s / 1e9, "unit": "GCUPS",
@@ -877,7 +900,8 @@ def run_manytomany(args, rank, world, local_rank):
                                    "1, even/odd symmetric prune, ckthr=1) in %dx%d blocks, "
                                    "X-drop x=49 in batches of %d" % (ns, nb, nb, bsz),
                        "mode": "xdrop"},
-            "candidates": {"pairs": ncand, "seconds": gen_s, "pairs_per_s": ncand / gen_s},
+            "candidates": {"pairs": ncand, "seconds": gen_s, "pairs_per_s": ncand / gen_s,
+                           "product_nnz": prod_nnz, "after_symmetric_prune": sym_nnz},
             "plain": {"seconds": plain_s, "alignments_per_s": ncand / plain_s,
                       "gcups": cells / plain_s / 1e9, "triples": ntrip},
             "tuned_filtered": {"seconds": filt_s, "alignments_per_s": ncand / filt_s,

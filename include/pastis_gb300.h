@@ -55,6 +55,10 @@ extern "C" {
 /* ---- behaviour flags */
 #define PG_F_SKIP_SPURIOUS_SEED 1 /* skip the (0,0) second seed of count==1 pairs
                                      (the reference extends it: SeqanXdropAligner.cpp:273-277) */
+#define PG_F_XDROP_AFFINE       2 /* X-drop extension with affine gaps (first / further gap
+                                     scores of the global alignment) instead of SeqAn's single
+                                     gap score (SeqanXdropAligner.cpp:281-283); a warp per
+                                     task, kept for a gap model that cannot be checked here */
 
 /* ---- per-pair result flags */
 #define PG_RF_EMPTY     1   /* no alignment columns (identity reported as 0) */

@@ -20,6 +20,7 @@ LETTERS = "ARNDCQEGHILKMFPSTWYVBZX*J"
 TIE_H_E_BEFORE_F = 1
 TIE_GAP_OPEN_FIRST = 2
 F_SKIP_SPURIOUS_SEED = 1
+F_XDROP_AFFINE = 2
 
 RF_EMPTY, RF_BAD_SEED, RF_PASSED = 1, 2, 4
 

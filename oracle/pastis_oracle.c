@@ -483,19 +483,129 @@ static uint64_t xdrop_dir(const uint8_t *vseq, int nv, int vstep,
     return cells;
 }
 
+/* The affine gap model of the same extension (switch ORC_F_XDROP_AFFINE).
+ * SeqAn's GappedXDrop extension takes a single gap score
+ * (SeqanXdropAligner.cpp:281-283 passes the aligner's Score object, whose
+ * scoreGap is the extend score); which model SeqAn applies cannot be run here,
+ * so this form is the other one.  It is Gotoh's three-state recurrence over
+ * the same anti-diagonals, a gap of length L scoring first + (L-1)*further as
+ * in the full DP (gap_first / gap_ext):
+ *   E(c, r) = max(T(c-1, r) + first, E(c-1, r) + further)    (V consumed)
+ *   F(c, r) = max(T(c, r-1) + first, F(c, r-1) + further)    (H consumed)
+ *   T(c, r) = max(T(c-1, r-1) + s, E(c, r), F(c, r))
+ * A cell whose T falls below best - X is dead in all three states.  The border
+ * cell of anti-diagonal d scores first + (d-1)*further (in T and in the gap
+ * state along its axis); border liveness, band trimming and the end point are
+ * those of the linear form with d*g replaced by that score.  With first ==
+ * further == g both forms compute the same cells. */
+static uint64_t xdrop_dir_affine(const uint8_t *vseq, int nv, int vstep,
+                                 const uint8_t *hseq, int nh, int hstep,
+                                 const orc_params *p, int *dv, int *dh)
+{
+    *dv = 0; *dh = 0;
+    const int cols = nv + 1, rows = nh + 1;
+    if (cols == 1 || rows == 1) return 0;
+    const int go = p->gap_first, ge = p->gap_ext, X = p->xdrop;
+    const int UND = NEG;
+    const size_t W = (size_t)cols + 1;
+    int *buf = (int *)malloc(sizeof(int) * 7 * W);
+    for (size_t k = 0; k < 7 * W; ++k) buf[k] = UND;
+    adiag A[3] = {{buf, 0, 0}, {buf + W, 0, 0}, {buf + 2 * W, 0, 0}};
+    adiag *a1 = &A[0], *a2 = &A[1], *a3 = &A[2];
+    int *E2 = buf + 3 * W, *E3 = buf + 4 * W, *F2 = buf + 5 * W, *F3 = buf + 6 * W;
+    uint64_t cells = 0;
+
+    /* d = 0: T(0,0) = 0; d = 1: the two border cells, T = first */
+    a2->off = 0; a2->len = 1; a2->v[0] = 0;
+    a3->off = 0; a3->len = 2;
+    {
+        const int v1 = (-go > X) ? UND : go;
+        a3->v[0] = a3->v[1] = v1;
+        F3[0] = v1;          /* (0, 1): a gap along H */
+        E3[1] = v1;          /* (1, 0): a gap along V */
+    }
+    int best = 0, d = 1, lo = 1, hi = 2;
+
+    while (lo < hi) {
+        ++d;
+        adiag *t = a1; a1 = a2; a2 = a3; a3 = t;
+        int *te = E2; E2 = E3; E3 = te;
+        int *tf = F2; F2 = F3; F3 = tf;
+        a3->off = lo - 1;
+        a3->len = hi + 1 - a3->off;
+        a3->v[a3->off] = UND; E3[a3->off] = UND; F3[a3->off] = UND;
+        a3->v[hi] = UND; E3[hi] = UND; F3[hi] = UND;
+        const long long bscore = (long long)go + (long long)(d - 1) * ge;
+        if (bscore > (long long)best - X) {
+            if (a3->off == 0) { a3->v[0] = (int)bscore; F3[0] = (int)bscore; }
+            if (d == hi && hi < cols) { a3->v[hi] = (int)bscore; E3[hi] = (int)bscore; }
+        }
+        int dbest = (int)(bscore < UND ? UND : bscore);
+        const int thr = best - X;
+        for (int c = lo; c < hi; ++c) {
+            const int r = d - c;
+            int e = a2->v[c - 1] + go;
+            if (E2[c - 1] + ge > e) e = E2[c - 1] + ge;
+            int f = a2->v[c] + go;
+            if (F2[c] + ge > f) f = F2[c] + ge;
+            const uint8_t vr = vseq[vstep * (c - 1)], hr = hseq[hstep * (r - 1)];
+            int tmp = a1->v[c - 1] + p->sm[vr * ORC_NRES + hr];
+            if (e > tmp) tmp = e;
+            if (f > tmp) tmp = f;
+            if (tmp < thr) { a3->v[c] = UND; E3[c] = UND; F3[c] = UND; }
+            else {
+                a3->v[c] = tmp; E3[c] = e; F3[c] = f;
+                if (tmp > dbest) dbest = tmp;
+            }
+        }
+        cells += (uint64_t)(hi - lo);
+        if (dbest > best) best = dbest;
+        while (lo - a3->off < a3->len && a3->v[lo] == UND &&
+               lo - a2->off - 1 < a2->len && a2->v[lo - 1] == UND)
+            ++lo;
+        while (hi - a3->off > 0 && a3->v[hi - 1] == UND && a2->v[hi - 1] == UND)
+            --hi;
+        ++hi;
+        if (lo < d + 2 - rows) lo = d + 2 - rows;
+        if (hi > cols) hi = cols;
+    }
+
+    int lc = a3->off + a3->len - 2;
+    int lr = d - lc;
+    int ls = a3->v[lc];
+    if (ls == UND) {
+        if (a2->v[a2->off + a2->len - 2] != UND) {
+            lc = a2->off + a2->len - 2; lr = d - 1 - lc; ls = a2->v[lc];
+        } else if (a2->len > 2 && a2->v[a2->off + a2->len - 3] != UND) {
+            lc = a2->off + a2->len - 3; lr = d - 1 - lc; ls = a2->v[lc];
+        }
+    }
+    if (ls == UND) {
+        for (int k = 0; k < a1->len; ++k) {
+            int val = a1->v[a1->off + k];
+            if (val > ls) { ls = val; lc = a1->off + k; lr = d - 2 - lc; }
+        }
+    }
+    if (ls != UND) { *dv = lc; *dh = lr; }
+    free(buf);
+    return cells;
+}
+
 uint64_t orc_xdrop_extend(const uint8_t *v, int m, const uint8_t *h, int n,
                           const orc_params *p, int *bh, int *eh, int *bv, int *ev)
 {
     int dv, dh;
     uint64_t cells = 0;
+    uint64_t (*dir)(const uint8_t *, int, int, const uint8_t *, int, int, const orc_params *,
+                    int *, int *) = (p->flags & ORC_F_XDROP_AFFINE) ? xdrop_dir_affine : xdrop_dir;
     /* left: prefixes V[0, bv), H[0, bh), consumed right to left */
     if (*bv > 0 && *bh > 0) {
-        cells += xdrop_dir(v + *bv - 1, *bv, -1, h + *bh - 1, *bh, -1, p, &dv, &dh);
+        cells += dir(v + *bv - 1, *bv, -1, h + *bh - 1, *bh, -1, p, &dv, &dh);
         *bv -= dv; *bh -= dh;
     }
     /* right: suffixes V[ev, m), H[eh, n) */
     if (*ev < m && *eh < n) {
-        cells += xdrop_dir(v + *ev, m - *ev, +1, h + *eh, n - *eh, +1, p, &dv, &dh);
+        cells += dir(v + *ev, m - *ev, +1, h + *eh, n - *eh, +1, p, &dv, &dh);
         *ev += dv; *eh += dh;
     }
     return cells;

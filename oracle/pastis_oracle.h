@@ -50,6 +50,7 @@ extern "C" {
 
 /* behaviour switches */
 #define ORC_F_SKIP_SPURIOUS_SEED 1 /* do not extend the second seed of a count==1 pair */
+#define ORC_F_XDROP_AFFINE       2 /* X-drop with affine gaps (gap_first / gap_ext) */
 
 /* result flags (same values as PG_RF_* in the product header) */
 #define ORC_RF_EMPTY     1  /* alignment has no columns; identity reported as 0 */

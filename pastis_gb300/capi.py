@@ -19,6 +19,7 @@ MODE_SW, MODE_XDROP = 0, 1
 GAPS_AS_CALLED, GAPS_NOMINAL = 0, 1
 TIE_H_E_BEFORE_F, TIE_GAP_OPEN_FIRST = 1, 2
 F_SKIP_SPURIOUS_SEED = 1
+F_XDROP_AFFINE = 2
 RF_EMPTY, RF_BAD_SEED, RF_PASSED, RF_FILTERED = 1, 2, 4, 8
 from .records import (KMERLIGHT_DTYPE, KMERLOC_DTYPE, LETTERS, NRES,  # noqa: F401
                       PAIR_DTYPE, RESULT_DTYPE, decode)

@@ -259,7 +259,8 @@ static int validate(const pg_config *c)
     if (c->seed_len < 1 || c->seed_len > 65535) return fail(PG_ERR_ARG, "seed_len %d", c->seed_len);
     if (c->seed_count < 0) return fail(PG_ERR_ARG, "seed_count %d", c->seed_count);
     if (c->tie < 0 || c->tie > 3) return fail(PG_ERR_ARG, "tie %d", c->tie);
-    if (c->flags & ~PG_F_SKIP_SPURIOUS_SEED) return fail(PG_ERR_ARG, "flags %d", c->flags);
+    if (c->flags & ~(PG_F_SKIP_SPURIOUS_SEED | PG_F_XDROP_AFFINE))
+        return fail(PG_ERR_ARG, "flags %d", c->flags);
     return PG_OK;
 }
 
@@ -374,12 +375,14 @@ static int ensure_scratch(pg_ctx *c)
     if (c->cfg.mode == PG_MODE_XDROP) {
         const int gw = (int)next_pow2((size_t)std::max(rmax, cmax) + 4);
         const size_t wwarps = (size_t)c->grid_wide * pg::WARPS;
+        // k_xd_wide keeps 3 anti-diagonals per warp, k_xda (affine gaps) 7
+        const size_t arrays = (c->cfg.flags & PG_F_XDROP_AFFINE) ? pg::XDA_ARRAYS : 3;
         if (gw > c->gring_w || wwarps > c->gring_warps || !c->d_gring) {
             cudaFree(c->d_gring);
             c->d_gring = nullptr;
             c->gring_w = 0;
             ++c->epoch;
-            CU(cudaMalloc(&c->d_gring, (size_t)3 * gw * sizeof(int) * wwarps));
+            CU(cudaMalloc(&c->d_gring, arrays * gw * sizeof(int) * wwarps));
             c->gring_w = gw;
             c->gring_warps = wwarps;
         }
@@ -616,8 +619,12 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
         if (c->tune.xd_blocks_per_sm > 0)
             xmax = std::min<uint64_t>(xmax, (uint64_t)c->nsm * (uint64_t)c->tune.xd_blocks_per_sm);
         const int gx = (int)std::min<uint64_t>(xmax, need_xd);
+        const bool affine = (c->cfg.flags & PG_F_XDROP_AFFINE) != 0;
         int xlaunch = 0;
-        if (!int16 && form == 2 && c->tune.bucket_order) {
+        if (affine) {
+            // affine gaps: a warp per task, one launch, nothing overflows
+            xlaunch = -1;
+        } else if (!int16 && form == 2 && c->tune.bucket_order) {
             // the extension tasks longest length bound first
             pg::KParams ko = kp;
             ko.xorder = c->d_xorder;
@@ -627,11 +634,15 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
             kp.xorder = c->d_xorder;
             xlaunch = 2;
         }
-        if (int16) pg::k_xd16<<<gx, pg::XT, 0, st>>>(kp);
-        else if (form == 2) pg::k_xdr<<<gx, pg::XT, 0, st>>>(kp);
-        else if (form == 1) pg::k_xdf<<<gx, pg::XT, 0, st>>>(kp);
-        else pg::k_xd<<<gx, pg::XT, 0, st>>>(kp);
-        pg::k_xd_wide<<<c->grid_wide, blk, 0, st>>>(kp);
+        if (affine) {
+            pg::k_xda<<<c->grid_wide, blk, 0, st>>>(kp);
+        } else {
+            if (int16) pg::k_xd16<<<gx, pg::XT, 0, st>>>(kp);
+            else if (form == 2) pg::k_xdr<<<gx, pg::XT, 0, st>>>(kp);
+            else if (form == 1) pg::k_xdf<<<gx, pg::XT, 0, st>>>(kp);
+            else pg::k_xd<<<gx, pg::XT, 0, st>>>(kp);
+            pg::k_xd_wide<<<c->grid_wide, blk, 0, st>>>(kp);
+        }
         if (kp.order) {
             pg::k_hist<true><<<gsched, 256, 0, st>>>(kp);
             pg::k_bucket<true><<<gsched, 256, 0, st>>>(kp);

@@ -38,6 +38,7 @@ namespace pg {
 
 constexpr int WARPS = 8;          // warps per block (k_ga, k_sw, k_xd_wide)
 constexpr int RING_W = 256;       // shared ring per warp in k_xd_wide
+constexpr int XDA_ARRAYS = 8;     // ring arrays per warp in k_xda (T x 3, E x 2, F x 2)
 constexpr int XT = 128;           // threads per block in k_xdf / k_xd16
 constexpr int XW = 16;            // per-thread ring slots in k_xdf
 

@@ -515,6 +515,64 @@ __global__ void __launch_bounds__(XT) k_xd16(const KParams kp)
     if (exec) atomicAdd(kp.exec_cells, exec);   // index 0 = X-drop cells
 }
 
+// ------------------------------------------------------------------ k_xda
+// The affine gap model of the extension (PG_F_XDROP_AFFINE): a warp per
+// (pair, seed) task taken from the work counter, both directions by
+// xdrop_dir_warp_affine on the warp's ring of 7 x gring_w ints in global
+// memory (L2-resident; gring_w covers the longest sequence, so no band
+// overflows).
+__global__ void __launch_bounds__(WARPS * 32) k_xda(const KParams kp)
+{
+    __shared__ int ssm[32 * 32];
+    load_sm(ssm, kp.sm);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint64_t gw = (uint64_t)blockIdx.x * WARPS + wib;
+    int *ring = kp.gring + gw * (uint64_t)XDA_ARRAYS * (uint64_t)kp.gring_w;
+    const uint64_t ntask = 2 * kp.n;
+    unsigned long long exec = 0;
+    for (;;) {
+        unsigned int tk = 0;
+        if (lane == 0) tk = atomicAdd(&kp.counter[1], 1u);
+        const uint64_t task = __shfl_sync(FULL, tk, 0);
+        if (task >= ntask) break;
+        const uint64_t p = task >> 1;
+        const int s = (int)(task & 1);
+        const pg_pair pr = kp.pairs[p];
+        XdRec rec{0, 0, 0, 0, 0u, 0u};
+        const uint8_t *V, *Hs;
+        int m, n;
+        if (!pair_seqs(kp, pr, V, m, Hs, n)) {
+            rec.flags = XF_BADIDX;
+        } else if (s >= kp.seed_count ||
+                   (s == 1 && (kp.flags & PG_F_SKIP_SPURIOUS_SEED) && pr.count < 2)) {
+            rec.flags = XF_NONE;
+        } else if (s == 1 && pr.rs1 == pr.rs0 && pr.cs1 == pr.cs0) {
+            rec.flags = XF_SAME;
+        } else {
+            int bv, ev, bh, eh;
+            if (seed_region(kp, pr, s, m, n, bv, ev, bh, eh)) rec.flags |= XF_BAD;
+            if (bv > 0 && bh > 0) {
+                const XdOut x = xdrop_dir_warp_affine(V + bv - 1, bv, -1, Hs + bh - 1, bh, -1, ssm,
+                                                      kp.go, kp.ge, kp.xdrop, ring, kp.gring_w);
+                rec.cells += x.cells;
+                bv -= x.dv; bh -= x.dh;
+            }
+            if (ev < m && eh < n) {
+                const XdOut x = xdrop_dir_warp_affine(V + ev, m - ev, 1, Hs + eh, n - eh, 1, ssm,
+                                                      kp.go, kp.ge, kp.xdrop, ring, kp.gring_w);
+                rec.cells += x.cells;
+                ev += x.dv; eh += x.dh;
+            }
+            rec.bv = (uint16_t)bv; rec.ev = (uint16_t)ev; rec.bh = (uint16_t)bh; rec.eh = (uint16_t)eh;
+            exec += rec.cells;
+        }
+        if (lane == 0) kp.xd[task] = rec;
+        __syncwarp();
+    }
+    if (lane == 0 && exec) atomicAdd(kp.exec_cells, exec);
+}
+
 __global__ void __launch_bounds__(WARPS * 32) k_xd_wide(const KParams kp)
 {
     __shared__ int ssm[32 * 32];

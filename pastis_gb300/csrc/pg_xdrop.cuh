@@ -131,6 +131,124 @@ __device__ inline XdOut xdrop_dir_warp(const uint8_t *__restrict__ V, int nv, in
     return o;
 }
 
+// The affine gap model of the extension (PG_F_XDROP_AFFINE), a warp per
+// direction: Gotoh's three states over the same anti-diagonals, a gap of
+// length L scoring go + (L-1)*ge,
+//   E(c, r) = max(T(c-1, r) + go, E(c-1, r) + ge)     (V consumed)
+//   F(c, r) = max(T(c, r-1) + go, F(c, r-1) + ge)     (H consumed)
+//   T(c, r) = max(T(c-1, r-1) + s, E(c, r), F(c, r))
+// with a dead T killing all three states; the border cell of anti-diagonal d
+// scores go + (d-1)*ge.  Band trimming and the end point are those of
+// xdrop_dir_warp.  The ring holds 7 arrays of W ints (T for three
+// anti-diagonals, E and F for two); W must cover the widest band (the caller
+// passes a power of two at least the longer sequence + 4).
+__device__ inline XdOut xdrop_dir_warp_affine(const uint8_t *__restrict__ V, int nv, int vstep,
+                                              const uint8_t *__restrict__ Hs, int nh, int hstep,
+                                              const int *__restrict__ ssm, int go, int ge, int X,
+                                              int *ring, int W)
+{
+    const int lane = threadIdx.x & 31;
+    XdOut o{0, 0, 0u, 1};
+    const int cols = nv + 1, rows = nh + 1;
+    if (cols == 1 || rows == 1) return o;
+    const int mask = W - 1;
+    int *A1 = ring, *A2 = ring + W, *A3 = ring + 2 * W;
+    int *E2 = ring + 3 * W, *E3 = ring + 4 * W, *F2 = ring + 5 * W, *F3 = ring + 6 * W;
+    int off1 = 0, len1 = 0, off2 = 0, len2 = 1, off3 = 0, len3 = 2;
+    if (lane == 0) {
+        A2[0] = 0;
+        const int v1 = (-go > X) ? UND : go;
+        A3[0] = v1; A3[1] = v1;
+        E3[0] = UND; F3[0] = v1;     // (0, 1): a gap along H
+        E3[1] = v1; F3[1] = UND;     // (1, 0): a gap along V
+    }
+    __syncwarp();
+    int best = 0, d = 1, lo = 1, hi = 2;
+    while (lo < hi) {
+        ++d;
+        int *t = A1; A1 = A2; A2 = A3; A3 = t;
+        t = E2; E2 = E3; E3 = t;
+        t = F2; F2 = F3; F3 = t;
+        off1 = off2; len1 = len2;
+        off2 = off3; len2 = len3;
+        off3 = lo - 1; len3 = hi + 1 - off3;
+        if (len3 > W) { o.ok = 0; return o; }
+        const int thr = best - X;
+        const long long bs = (long long)go + (long long)(d - 1) * ge;
+        const int bscore = bs < UND ? UND : (int)bs;
+        int lbest = bscore;
+        for (int c = lo + lane; c < hi; c += 32) {
+            const int r = d - c;
+            const int e = max(A2[(c - 1) & mask] + go, E2[(c - 1) & mask] + ge);
+            const int f = max(A2[c & mask] + go, F2[c & mask] + ge);
+            const int vr = __ldg(V + vstep * (c - 1));
+            const int hr = __ldg(Hs + hstep * (r - 1));
+            const int v = max(A1[(c - 1) & mask] + ssm[vr * 32 + hr], max(e, f));
+            const bool live = v >= thr;
+            A3[c & mask] = live ? v : UND;
+            E3[c & mask] = live ? e : UND;
+            F3[c & mask] = live ? f : UND;
+            if (live) lbest = max(lbest, v);
+        }
+        if (lane == 0) {
+            const int bval = ((long long)bscore > (long long)best - X) ? bscore : UND;
+            const int lo_t = (off3 == 0) ? bval : UND;
+            A3[off3 & mask] = lo_t; E3[off3 & mask] = UND; F3[off3 & mask] = lo_t;
+            const int hi_t = (d == hi && hi < cols) ? bval : UND;
+            A3[hi & mask] = hi_t; E3[hi & mask] = hi_t; F3[hi & mask] = UND;
+        }
+        __syncwarp();
+        const int db = __reduce_max_sync(FULL, lbest);
+        if (db > best) best = db;
+        o.cells += (uint32_t)(hi - lo);
+        for (int c0 = lo;; c0 += 32) {
+            const int c = c0 + lane;
+            bool cond = (c - off3 < len3);
+            if (cond) cond = A3[c & mask] == UND;
+            if (cond) cond = (c - off2 - 1 < len2);
+            if (cond) cond = A2[(c - 1) & mask] == UND;
+            const unsigned bal = __ballot_sync(FULL, !cond);
+            if (bal) { lo = c0 + __ffs(bal) - 1; break; }
+        }
+        for (int c0 = hi;; c0 -= 32) {
+            const int c = c0 - lane;
+            bool cond = (c - off3 > 0);
+            if (cond) cond = A3[(c - 1) & mask] == UND;
+            if (cond) cond = A2[(c - 1) & mask] == UND;
+            const unsigned bal = __ballot_sync(FULL, !cond);
+            if (bal) { hi = c0 - (__ffs(bal) - 1); break; }
+        }
+        ++hi;
+        if (lo < d + 2 - rows) lo = d + 2 - rows;
+        if (hi > cols) hi = cols;
+        __syncwarp();
+    }
+
+    int lc = off3 + len3 - 2, lr = d - lc, ls = A3[lc & mask];
+    if (ls == UND) {
+        const int ca = off2 + len2 - 2;
+        if (A2[ca & mask] != UND) {
+            lc = ca; lr = d - 1 - lc; ls = A2[ca & mask];
+        } else if (len2 > 2 && A2[(ca - 1) & mask] != UND) {
+            lc = ca - 1; lr = d - 1 - lc; ls = A2[(ca - 1) & mask];
+        }
+    }
+    if (ls == UND) {
+        int bv = UND, bc = 0x7fffffff;
+        for (int k = lane; k < len1; k += 32) {
+            const int val = A1[(off1 + k) & mask];
+            if (val > bv) { bv = val; bc = off1 + k; }
+        }
+        const int mv = __reduce_max_sync(FULL, bv);
+        const unsigned cand = (bv == mv) ? (unsigned)bc : 0x7fffffffu;
+        const int mc = (int)__reduce_min_sync(FULL, cand);
+        if (mv != UND) { ls = mv; lc = mc; lr = d - 2 - lc; }
+    }
+    if (ls != UND) { o.dv = lc; o.dh = lr; }
+    __syncwarp();
+    return o;
+}
+
 // The same extension run by one thread from start to end (k_xd).  The ring
 // holds W ints per
 // anti-diagonal; slot (array k, column c) sits at base[(k*W + (c & (W-1))) * NT]
