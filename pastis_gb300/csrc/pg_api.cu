@@ -326,7 +326,7 @@ int pg_create(const pg_config *cfg, pg_ctx **out)
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pr, pg::k_xd, pg::XT, 0));
         c->grid_xd_run = c->nsm * std::max(pr, 1);
         int pq = 0;
-        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pq, pg::k_xdr, pg::XT, 0));
+        CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pq, pg::k_xdr<8>, pg::XT, 0));
         c->grid_xdr = c->nsm * std::max(pq, 1);
         CUD(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pw, pg::k_xd_wide, pg::WARPS * 32, 0));
         c->grid_xd = c->nsm * std::max(px, 1);
@@ -638,7 +638,7 @@ static int launch(pg_ctx *c, const pg_pair *d_pairs, uint64_t n, uint64_t roff, 
             pg::k_xda<<<c->grid_wide, blk, 0, st>>>(kp);
         } else {
             if (int16) pg::k_xd16<<<gx, pg::XT, 0, st>>>(kp);
-            else if (form == 2) pg::k_xdr<<<gx, pg::XT, 0, st>>>(kp);
+            else if (form == 2) pg::k_xdr<8><<<gx, pg::XT, 0, st>>>(kp);
             else if (form == 1) pg::k_xdf<<<gx, pg::XT, 0, st>>>(kp);
             else pg::k_xd<<<gx, pg::XT, 0, st>>>(kp);
             pg::k_xd_wide<<<c->grid_wide, blk, 0, st>>>(kp);

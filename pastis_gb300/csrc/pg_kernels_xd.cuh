@@ -314,12 +314,18 @@ __global__ void __launch_bounds__(256) k_xtask_bucket(const KParams kp)
 
 // ------------------------------------------------------------------ k_xdr
 // One thread per (pair, seed) task with the band window in registers
-// (XrDir): every step computes the 16 window columns with packed 16-bit
+// (XrDirT<NW>): every step computes the 2 NW window columns with packed 16-bit
 // operations and no branch on the band, so a warp's threads step together
-// whatever their band widths.  Tasks are taken and their inputs read ahead as
-// in k_xdf; a direction starts the moment the previous one ends.  A window
-// wider than 15 columns sends the task to the overflow list for k_xd_wide.
+// whatever their band widths.  Tasks are taken (longest length bound first
+// when kp.xorder is set) and their inputs read ahead as in k_xdf; a direction
+// starts the moment the previous one ends.  A window wider than 2 NW - 1
+// columns sends the task to the overflow list for k_xd_wide.  NW = 8 runs:
+// a 12-slot window (NW = 6) executed 15 % fewer instructions on xdrop1m, but
+// the 4 % of tasks that outgrew it, rerun on 16 slots in a launch of their
+// own, were long homolog extensions at a tenth of the warps, and the
+// extension took 9.85 ms per 1M pairs against 9.3.
 // Needs xdr_supported(xg, xdrop).
+template <int NW>
 __global__ void __launch_bounds__(XT) k_xdr(const KParams kp)
 {
     __shared__ int ssm[PG_NRES * XR_STRIDE];
@@ -364,7 +370,7 @@ __global__ void __launch_bounds__(XT) k_xdr(const KParams kp)
         ta = fetch();
     }
 
-    XrDir dir;
+    XrDirT<NW> dir;
     XdRec rec{0, 0, 0, 0, 0u, 0u};
     uint32_t task = 0;
     const uint8_t *V = nullptr, *Hs = nullptr;

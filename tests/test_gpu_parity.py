@@ -88,6 +88,29 @@ def test_xdrop_parity(xd_small, oracle_mod, tie, gaps):
     assert (got["seed_used"] == 1).any() and (got["flags"] & capi.RF_PASSED).any()
 
 
+@pytest.mark.parametrize("gaps,xdrop", [(0, 49), (1, 49), (0, 200), (0, 10), (0, 0)])
+def test_register_window_extension(xd_small, oracle_mod, gaps, xdrop):
+    """The register-window extension gives the oracle's results, also where
+    most windows overflow it (the nominal gaps, X = 200) and the warp kernel
+    takes the rest."""
+    from pastis_gb300 import capi
+    w = xd_small
+    cfg = capi.config(capi.MODE_XDROP, gap_semantics=gaps, xdrop=xdrop)
+    ctx = capi.Context(cfg)
+    ctx.set_seqs(0, w.ascii, w.offs)
+    ctx.share_row_seqs()
+    ctx.set_tuning(xd_stepped=2)
+    got = ctx.align(w.pairs)
+    # order (2), k_xdr, k_xd_wide, then the traceback form's k_hist, k_bucket,
+    # k_dirsize, k_ga_dir, k_ga_pair, k_tb_ga
+    assert ctx.last_launches() in (10, 11)
+    ctx.close()
+    O = oracle_mod
+    codes = O.encode(bytes(w.ascii))
+    exp = O.batch(1, codes, w.offs, codes, w.offs, w.pairs, oracle_params(O, cfg))
+    assert_same(got, exp, w.pairs)
+
+
 @pytest.mark.parametrize("flags,xdrop,seed_count", [(1, 49, 2), (0, 10, 2), (0, 200, 2),
                                                       (0, 49, 1), (0, 0, 2)])
 def test_xdrop_switches(xd_small, oracle_mod, flags, xdrop, seed_count):
