@@ -3,13 +3,14 @@
 // The same direction as xdrop_dir_thread (pg_xdrop.cuh), restating
 // seqan::extendSeed(..., GappedXDrop()) as src/align/SeqanXdropAligner.cpp:281-283
 // calls it, with identical band cells, end point and cell count, but with a
-// different machine shape.  One thread holds a window of NS = 16 or 12
-// anti-diagonal columns in registers: column c lives in slot c mod NS, two
-// slots per 32-bit register (slot 2k in the low half, 2k+1 in the high half),
-// as int16 values relative to a base B that moves up by RB when the best score
-// passes B + RB.  Every step computes all NS slots with packed 16-bit max/add
-// (two cells per instruction), without a branch on the band.  This is exact
-// because a cell outside the band [lo, hi) always comes out dead:
+// different machine shape.  One thread holds a window of NS = 2 NW
+// anti-diagonal columns in registers (k_xdr uses NW = 8: 16 columns): column c
+// lives in slot c mod NS, two slots per 32-bit register (slot 2k in the low
+// half, 2k+1 in the high half), as int16 values relative to a base B that
+// moves up by RB when the best score passes B + RB.  Every step computes all
+// NS slots with packed 16-bit max/add (two cells per instruction), without a
+// branch on the band.  This is exact because a cell outside the band [lo, hi)
+// always comes out dead:
 //   - columns left of lo were trimmed (dead, with a dead left neighbour one
 //     anti-diagonal back), columns right of hi have only dead predecessors,
 //     cells with r < 0 have none; so the recurrence gives them nothing live;
