@@ -59,6 +59,41 @@ def test_candidates_errors(fam):
     ctx.close()
 
 
+def test_product_and_prune_counts(fam):
+    """The counts the many-to-many bench reports (the reference's c_nnz and
+    prune_sym log lines): on a diagonal block the product is symmetric, so it
+    holds twice the even/odd-pruned pairs plus one diagonal entry per sequence
+    with a k-mer; the ckthr prune only removes pairs; a count-only call
+    (no output buffer) agrees with the materialised candidates."""
+    import ctypes
+
+    from pastis_gb300 import capi
+    ctx = capi.Context(capi.config(capi.MODE_XDROP))
+    ctx.set_seqs(0, fam.ascii, fam.offs)
+    ctx.share_row_seqs()
+    blk = (0, 200)
+
+    def count(prune, ckthr):
+        kc = capi.kmer_config(k=6, stride=1, prune=prune, ckthr=ckthr)
+        n = ctypes.c_uint64()
+        rc = ctx.lib.pg_candidates(ctx.h, ctypes.byref(kc), blk[0], blk[1], blk[0], blk[1], None,
+                                   0, ctypes.byref(n), None)
+        assert rc in (capi.PG_OK, capi.PG_ERR_RANGE)
+        return int(n.value)
+
+    full = ctx.candidates(capi.kmer_config(k=6, stride=1, prune=capi.PRUNE_NONE), blk, blk)
+    eo = ctx.candidates(capi.kmer_config(k=6, stride=1, prune=capi.PRUNE_EVEN_ODD), blk, blk)
+    diag = int((full["row"] == full["col"]).sum())
+    L = fam.lengths()[blk[0]:blk[1]]
+    assert diag == int((L >= 6).sum())
+    assert len(full) == 2 * len(eo) + diag
+    assert count(capi.PRUNE_NONE, 0) == len(full)
+    assert count(capi.PRUNE_EVEN_ODD, 0) == len(eo)
+    thr = count(capi.PRUNE_EVEN_ODD, 1)
+    assert thr == int((eo["count"] > 1).sum()) and thr < len(eo)
+    ctx.close()
+
+
 def test_triples_are_the_nonzero_score_aln_entries(fam):
     """Candidates -> alignment -> triples, all on the device; the triples equal
     the host-side selection of score_aln != 0 with block offsets added."""
