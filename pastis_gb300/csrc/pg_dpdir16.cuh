@@ -26,9 +26,10 @@
 // A local alignment's floor needs no bit: the traceback carries the score of
 // the cell it stands on and stops where H is 0, which is where the 32-bit
 // form sets its zero code.  Layout: the nibbles of virtual lane v's R rows at
-// column j in word (stripe * (n + 63) + k) * 64 + v, k = j - 1 + v; a lane
-// stores its two virtual lanes' words as one 8-byte store, so a warp writes
-// 256 contiguous bytes per step.
+// column j in word dir16_warp_word(stripe, k, v, n), k = j - 1 + v: a lane
+// stores its two virtual lanes' words as one 8-byte store, and its stores of
+// 4 consecutive steps fill one 32-byte sector (a traceback along a lane reads
+// a new sector every few moves).
 //
 // Borders need no special case in the loop.  The high half starts one column
 // early, at column 0, from a column -1 of sentinels (H = NEG16) and the
@@ -106,11 +107,24 @@ __host__ __device__ __forceinline__ int dir16_rows(int m, int cap)
     return r < 1 ? 1 : r;
 }
 
+// A stripe's wavefront steps, rounded up to whole 4-step tiles
+__host__ __device__ __forceinline__ int dir16_steps(int n) { return (n + 63 + 3) & ~3; }
+
 __host__ __device__ __forceinline__ uint64_t dir16_bytes(int m, int n, int R)
 {
     if (m <= 0 || n <= 0) return 0;
     const uint64_t stripes = (uint64_t)((m + 64 * R - 1) / (64 * R));
-    return stripes * (uint64_t)(n + 63) * 256ull;
+    return stripes * (uint64_t)dir16_steps(n) * 256ull;
+}
+
+// Word (32-bit) index of virtual lane v (0..63) at wavefront step k of stripe s
+// in a whole-warp region: tiles of 4 steps, each lane's 8-byte words (its two
+// virtual lanes) of the 4 steps filling one 32-byte sector, so that a
+// traceback walk along a lane reads a new sector every few moves
+__host__ __device__ __forceinline__ uint64_t dir16_warp_word(int s, int k, int v, int n)
+{
+    return ((((uint64_t)s * (uint64_t)(dir16_steps(n) >> 2) + (uint64_t)(k >> 2)) * 32u +
+             (uint64_t)(v >> 1)) * 4u + (uint64_t)(k & 3)) * 2u + (uint64_t)(v & 1);
 }
 
 // prmt selectors: row q of each half's word, sign-extended to 16 bits
@@ -204,7 +218,8 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
             const int j1 = -2 * lane + 1;                // low half's column at step 0
             if (j1 >= 1 && j1 <= n) hc_next = (int)__ldg(Hs + j1 - 1);
         }
-        uint2 *dstep = reinterpret_cast<uint2 *>(dir) + (uint64_t)stripe * (uint64_t)(n + 63) * 32u + lane;
+        uint2 *dtile = reinterpret_cast<uint2 *>(dir) +
+                       (uint64_t)stripe * (uint64_t)(dir16_steps(n) >> 2) * 128u + lane * 4;
         uint32_t sbs = 0, sbs_seen = 0;
         int sbp0 = 0, sbp1 = 0;
         const int nsteps = n + v_last;
@@ -267,7 +282,8 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
                     if (LOCAL) sbs = v16max(sbs, Hv);
                     if (CHECK && !LOCAL) { hmn = v16min(hmn, Hv); hmx = v16max(hmx, Hv); }
                 }
-                dstep[(uint64_t)k * 32u] = make_uint2(prmt(W0, W1, 0x5410u), prmt(W0, W1, 0x7632u));
+                dtile[(uint64_t)(k >> 2) * 128u + (uint64_t)(k & 3)] =
+                    make_uint2(prmt(W0, W1, 0x5410u), prmt(W0, W1, 0x7632u));
                 out_h = Hl[R - 1];
                 out_a = cA;
                 if (!last_block && lane == t_last) {

@@ -38,9 +38,9 @@ struct TraceOut {
 // carries the score of the cell it stands on, h, and stops where it is 0).
 // Otherwise the nibbles of dp_warp_dir (bits 0-1: diagonal, F, E or the local
 // floor).  Words: (s * (n + vl - 1) + k) * vl + v for stripe s, wavefront step
-// k = j - 1 + v, lane v (vl = 32 lanes or 64 virtual lanes of a warp); the
-// half-warp regions of dp_pair_dir16 (W16, vl = 32) lie in 4-step tiles
-// (dir16_pair_word).  ssm: the 32 x 32 substitution table in shared memory (read only
+// k = j - 1 + v, lane v (vl = 32 lanes of dp_warp_dir); the 16-bit regions
+// lie in 4-step tiles (dir16_pair_word for the half-warp regions of
+// dp_pair_dir16, vl = 32; dir16_warp_word for the whole-warp ones, vl = 64).  ssm: the 32 x 32 substitution table in shared memory (read only
 // by a local W16 walk).  step() makes one move and returns false once the walk
 // has ended; the counts are then final.
 template <bool LOCAL, bool W16>
@@ -90,8 +90,8 @@ struct Walker {
         }
         // the word of (i, j) first (i, j >= 1 here): its load does not wait on h,
         // whose substitution-score lookups it overlaps
-        const uint64_t widx = (W16 && vl == 32) ? dir16_pair_word(j - 1 + v, v)
-                              : ((uint64_t)s * (uint64_t)(n + vl - 1) + (uint64_t)(j - 1 + v)) * (uint64_t)vl + v;
+        const uint64_t widx = !W16 ? ((uint64_t)s * (uint64_t)(n + vl - 1) + (uint64_t)(j - 1 + v)) * (uint64_t)vl + v
+                              : vl == 32 ? dir16_pair_word(j - 1 + v, v) : dir16_warp_word(s, j - 1 + v, v, n);
         const uint32_t w = __ldg(dir + widx);
         if (LOCAL) {
             // the walk moves back through the wavefront steps: ask L1 now for
