@@ -93,12 +93,12 @@ struct Walker {
         const uint64_t widx = !W16 ? ((uint64_t)s * (uint64_t)(n + vl - 1) + (uint64_t)(j - 1 + v)) * (uint64_t)vl + v
                               : vl == 32 ? dir16_pair_word(j - 1 + v, v) : dir16_warp_word(s, j - 1 + v, v, n);
         const uint32_t w = __ldg(dir + widx);
-        if (LOCAL) {
+        {
             // the walk moves back through the wavefront steps: ask L1 now for
             // the word 1 KiB back in either layout (8 steps of the half-warp
             // tiles, 4 steps of the others), so that its sector is there when
-            // the walk arrives (sw100k traceback 9.13 -> 9.02 ms per step; the
-            // X-drop walks measured no faster)
+            // the walk arrives (sw100k 9.13 -> 9.02 ms per step; xdrop1m
+            // alignment 40.27 -> 40.16 ms with every 16-bit region tiled)
             const uint64_t back = (W16 && vl == 32) ? 256u : 4u * (uint64_t)vl;
             if (widx >= back) asm volatile("prefetch.global.L1 [%0];" :: "l"(dir + widx - back));
         }
