@@ -220,6 +220,12 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
         }
         uint2 *dtile = reinterpret_cast<uint2 *>(dir) +
                        (uint64_t)stripe * (uint64_t)(dir16_steps(n) >> 2) * 128u + lane * 4;
+        // local form: a lane's words go out two steps at a time, 16 bytes (an
+        // even step's word waits in wprev for the odd step after it; wk = its
+        // step, -1: none).  uneven10m_sw 11.94 -> 11.66 s, sw100k 8.97 -> 8.94
+        // ms; the global form measured slower that way (xdrop1m 40.1 -> 43.0 ms)
+        uint2 wprev = make_uint2(0u, 0u);
+        int wk = -1;
         uint32_t sbs = 0, sbs_seen = 0;
         int sbp0 = 0, sbp1 = 0;
         const int nsteps = n + v_last;
@@ -282,8 +288,18 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
                     if (LOCAL) sbs = v16max(sbs, Hv);
                     if (CHECK && !LOCAL) { hmn = v16min(hmn, Hv); hmx = v16max(hmx, Hv); }
                 }
-                dtile[(uint64_t)(k >> 2) * 128u + (uint64_t)(k & 3)] =
-                    make_uint2(prmt(W0, W1, 0x5410u), prmt(W0, W1, 0x7632u));
+                const uint2 wd = make_uint2(prmt(W0, W1, 0x5410u), prmt(W0, W1, 0x7632u));
+                if (!LOCAL) {
+                    dtile[(uint64_t)(k >> 2) * 128u + (uint64_t)(k & 3)] = wd;
+                } else if (k & 1) {
+                    uint2 *dst = dtile + (uint64_t)(k >> 2) * 128u + (uint64_t)(k & 2);
+                    if (wk >= 0) *reinterpret_cast<uint4 *>(dst) = make_uint4(wprev.x, wprev.y, wd.x, wd.y);
+                    else dst[1] = wd;
+                    wk = -1;
+                } else {
+                    wprev = wd;
+                    wk = k;
+                }
                 out_h = Hl[R - 1];
                 out_a = cA;
                 if (!last_block && lane == t_last) {
@@ -312,6 +328,9 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
                     }
                     sbs_seen = sbs;
                 }
+            } else if (LOCAL && wk >= 0) {
+                dtile[(uint64_t)(wk >> 2) * 128u + (uint64_t)(wk & 3)] = wprev;
+                wk = -1;
             }
         };
         if (LOCAL) {
@@ -323,6 +342,7 @@ __device__ DirOut dp_warp_dir16(const uint8_t *__restrict__ V, int m,
         } else {
             for (int k = 0; k < nsteps; ++k) step(k);
         }
+        if (LOCAL && wk >= 0) dtile[(uint64_t)(wk >> 2) * 128u + (uint64_t)(wk & 3)] = wprev;
         __syncwarp();
         if (CHECK && LOCAL) lmx = v16max(lmx, sbs);
         if (LOCAL) {
@@ -467,6 +487,9 @@ __device__ DirOut dp_pair_dir16(const uint8_t *__restrict__ V, int m,
         if (j1 >= 1 && j1 <= n) hc_next = (int)__ldg(Hs + j1 - 1);
     }
     uint2 *dtile = reinterpret_cast<uint2 *>(dir) + sl * 4;
+    // local form: a lane's words go out two steps at a time, as in dp_warp_dir16
+    uint2 wprev = make_uint2(0u, 0u);
+    int wk = -1;
     uint32_t sbs = 0, sbs_seen = 0;
     int sbp0 = 0, sbp1 = 0;
     int nsteps = has ? n + v_last : 0;
@@ -520,8 +543,18 @@ __device__ DirOut dp_pair_dir16(const uint8_t *__restrict__ V, int m,
                 Gl[r] = G;
                 if (LOCAL) sbs = v16max(sbs, Hv);
             }
-            dtile[(uint64_t)(k >> 2) * 64u + (uint64_t)(k & 3)] =
-                make_uint2(prmt(W0, W1, 0x5410u), prmt(W0, W1, 0x7632u));
+            const uint2 wd = make_uint2(prmt(W0, W1, 0x5410u), prmt(W0, W1, 0x7632u));
+            if (!LOCAL) {
+                dtile[(uint64_t)(k >> 2) * 64u + (uint64_t)(k & 3)] = wd;
+            } else if (k & 1) {
+                uint2 *dst = dtile + (uint64_t)(k >> 2) * 64u + (uint64_t)(k & 2);
+                if (wk >= 0) *reinterpret_cast<uint4 *>(dst) = make_uint4(wprev.x, wprev.y, wd.x, wd.y);
+                else dst[1] = wd;
+                wk = -1;
+            } else {
+                wprev = wd;
+                wk = k;
+            }
             out_h = Hl[R - 1];
             out_a = cA;
             if (LOCAL && sbs != sbs_seen) {
@@ -539,6 +572,9 @@ __device__ DirOut dp_pair_dir16(const uint8_t *__restrict__ V, int m,
                 }
                 sbs_seen = sbs;
             }
+        } else if (LOCAL && wk >= 0) {
+            dtile[(uint64_t)(wk >> 2) * 64u + (uint64_t)(wk & 3)] = wprev;
+            wk = -1;
         }
     };
     if (LOCAL) {
@@ -550,6 +586,7 @@ __device__ DirOut dp_pair_dir16(const uint8_t *__restrict__ V, int m,
     } else {
         for (int k = 0; k < nsteps; ++k) step(k);
     }
+    if (LOCAL && wk >= 0) dtile[(uint64_t)(wk >> 2) * 64u + (uint64_t)(wk & 3)] = wprev;
     __syncwarp();
     DirOut res;
     res.have = 0; res.ei = 0; res.ej = 0; res.score = 0;
