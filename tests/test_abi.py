@@ -74,10 +74,16 @@ def test_create_rejects_bad_config(native):
     lib = capi.load()
     h = ctypes.c_void_p()
     for field, val in (("mode", 7), ("tie", 9), ("xdrop", -1), ("gap_open", -5000),
-                       ("seed_len", 0), ("flags", 64)):
+                       ("seed_len", 0), ("flags", 64), ("flags", 4)):
         c = capi.config(capi.MODE_XDROP)
         setattr(c, field, val)
         assert lib.pg_create(ctypes.byref(c), ctypes.byref(h)) == capi.PG_ERR_ARG, field
+    # the two defined flags pass validation (and then find no device here)
+    c = capi.config(capi.MODE_XDROP, flags=capi.F_SKIP_SPURIOUS_SEED | capi.F_XDROP_AFFINE)
+    rc = lib.pg_create(ctypes.byref(c), ctypes.byref(h))
+    assert rc != capi.PG_ERR_ARG
+    if rc == capi.PG_OK:
+        lib.pg_destroy(h)
 
 
 def test_noalloc_argument_checks_without_gpu(native):
